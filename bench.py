@@ -1,0 +1,371 @@
+"""Benchmark of the fused render-path training step (forward + MSE + backward).
+
+Workload (dense 256^3 fp32 RGBA grid, 16 Gaussian blobs, box [-1.5,1.5]^3; 100 cameras of
+800x800 at radius 4 on the upper hemisphere, FOV 0.691 rad; 8192 random rays per step
+spread camera-major over the cameras, near 2, far 6, 256 stratified samples per ray,
+trilinear lookup). Synthetic seeded data stands in for the NeRF-synthetic scenes.
+
+A step = zero the dense gradient + one fused kernel that generates the rays from the
+resident cameras and images, samples, looks up, composites, takes the MSE gradient and
+scatters dL/dcell. `value` is rays/s with everything resident in HBM; `e2e` is the same
+metric through FusedTrainStep.step_rays with the ray batch (origins, dirs, targets)
+copied from pinned host memory every step and the loss copied back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`--impl reference` times the reference's algorithm on the host CPU (the oracle's
+restatement of it in PyTorch ops, all host threads) on a bounded sample of the same
+workload. Under torchrun with N > 1 each rank trains on its own ray batch with a
+replicated grid and the gradients are summed with one all-reduce per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import scenes  # noqa: E402  (seeded synthetic scene builder)
+
+WORKLOAD = dict(workload="train step, 256^3 fp32 grid, 100 cams 800x800, 8192 rays x 256 "
+                         "stratified samples, trilinear", grid=256, cameras=100, image=800,
+                rays=8192, samples=256, mode="trilinear", near=2.0, far=6.0, blobs=16,
+                camera_angle_x=0.691)
+METRIC = "train rays/sec (fwd+bwd)"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_scene(dev, W):
+    side = W["grid"]
+    grid = torch.from_numpy(scenes.make_grid(side, W["blobs"], seed=1)).to(dev)
+    T = torch.from_numpy(scenes.make_cameras(W["cameras"], seed=2)).to(dev)
+    # targets: 100 x 800 x 800 RGBA fp32 = 1 GiB resident, seeded on the device
+    g = torch.Generator(device=dev).manual_seed(3)
+    imgs = torch.rand(W["cameras"], W["image"], W["image"], 4, device=dev, generator=g)
+    return grid, T, imgs
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def unique_cells(pg, grid, T, imgs, W, seed, delta, pd):
+    """U: distinct cells the step's in-bounds samples read (from the kernels' own index
+    math), the per-unit figure of the algorithmic byte count."""
+    idx, inb = pg.render.camera_sample_indices(
+        grid, T, imgs, W["camera_angle_x"], W["rays"], seed, W["near"], delta, W["samples"], pd,
+        mode=W["mode"], stratified=True, seed=7)
+    side = W["grid"]
+    lin = (idx[..., 0] * side + idx[..., 1]) * side + idx[..., 2]
+    lin = lin[inb] if W["mode"] == "nearest" else lin[inb.unsqueeze(-1).expand_as(lin)]
+    return int(torch.unique(lin).numel()), float(inb.float().mean())
+
+
+def cpu_reference_rate(W, grid_cpu, T_cpu, imgs_cpu, budget_s=12.0, rays=1024):
+    """The reference's path on the host cores: oracle port, fp32 autograd, all threads.
+    Bounded sample: `rays` rays per step of the same scene and sampling, repeated until
+    budget_s of work (at least 2 timed steps after one warm-up)."""
+    from oracle import torch_port as tp
+    torch.set_num_threads(os.cpu_count() or 1)
+    pd = 3.0 / W["grid"]
+    S = W["samples"]
+    delta = (W["far"] - W["near"]) / S
+    gmin = tp.grid_min(grid_cpu.shape, pd)
+
+    def one(step):
+        o, d, target = tp.camera_batch(T_cpu, W["camera_angle_x"], imgs_cpu, rays, 1000 + step,
+                                       W["near"])
+        jit = tp.jitter_for(7, rays, S)
+        g = grid_cpu.detach().requires_grad_(True)
+        t0 = time.perf_counter()
+        loss = tp.train_loss(g, o, d, target, S, delta, gmin, pd, W["mode"], True, jit)
+        loss.backward()
+        return time.perf_counter() - t0
+
+    one(0)
+    times = []
+    start = time.perf_counter()
+    while len(times) < 2 or (time.perf_counter() - start < budget_s and len(times) < 20):
+        times.append(one(len(times) + 1))
+    med = statistics.median(times)
+    return dict(value=rays / med, unit="rays/s", cores=torch.get_num_threads(), kind="port",
+                sample=f"{rays} rays/step of the same workload (256^3 grid, 256 stratified samples, "
+                       f"trilinear), fwd+bwd, median of {len(times)} steps after 1 warm-up; "
+                       "oracle restatement in torch CPU ops, fp32")
+
+
+def torch_gpu_rate(W, grid, T, imgs, dev, steps=3):
+    """The reference's algorithm as plain torch ops on the same GPU (oracle port with
+    CUDA tensors; CUDA-event timed)."""
+    from oracle import torch_port as tp
+    pd = 3.0 / W["grid"]
+    S = W["samples"]
+    R = W["rays"]
+    delta = (W["far"] - W["near"]) / S
+    gmin = tp.grid_min(grid.shape, pd).to(dev)
+    o, d, target = tp.camera_batch(T.cpu(), W["camera_angle_x"], imgs.cpu(), R, 4242, W["near"])
+    o, d, target = o.to(dev), d.to(dev), target.to(dev)
+    jit = tp.jitter_for(7, R, S).to(dev)
+
+    def one():
+        g = grid.detach().requires_grad_(True)
+        loss = tp.train_loss(g, o, d, target, S, delta, gmin, pd, W["mode"], True, jit)
+        loss.backward()
+
+    one()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        one()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / steps
+    return dict(value=R / (ms / 1e3), unit="rays/s", ms_per_step=ms, kind="port",
+                sample=f"{R} rays x {S} samples, same scene, {steps} steps after 1 warm-up")
+
+
+def run_reference_arm(args, W):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    grid = torch.from_numpy(scenes.make_grid(W["grid"], W["blobs"], seed=1))
+    T = torch.from_numpy(scenes.make_cameras(W["cameras"], seed=2))
+    g = torch.Generator().manual_seed(3)
+    imgs = torch.rand(W["cameras"], W["image"], W["image"], 4, generator=g)
+    per_step = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_reference_rate(W, grid, T, imgs, budget_s=4.0, rays=512)
+        if i >= args.warmup:
+            per_step.append(r["value"])
+            cb = r
+    value = statistics.median(per_step)
+    cb["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * W["rays"] / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": dict(W, step="per step a bounded sample of 512 rays; ms_per_step scaled to "
+                                   "8192 rays"),
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and torch-GPU legs")
+    args = ap.parse_args()
+    W = dict(WORKLOAD)
+
+    if args.impl == "reference":
+        run_reference_arm(args, W)
+        return
+
+    import plenoxels_gb300 as pg
+    import plenoxels_gb300.render  # noqa: F401
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    S, R = W["samples"], W["rays"]
+    pd = 3.0 / W["grid"]
+    delta = (W["far"] - W["near"]) / S
+    grid, T, imgs = build_scene(dev, W)
+    step = pg.FusedTrainStep(grid, pd, S, delta, mode=W["mode"], stratified=True, seed=7)
+    stream = torch.cuda.current_stream(dev)
+
+    def train(i):
+        step.step_cameras(T, imgs, W["camera_angle_x"], R, 1000 * rank + i, near=W["near"])
+        if world > 1:
+            torch.distributed.all_reduce(step.grad)
+
+    for i in range(args.warmup):
+        train(i)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+
+    # timed region: K steps, per-kernel events around the fused kernel
+    k_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    k_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = pg.launch_count()
+    with Clocks(dev.index) as clk:
+        time.sleep(0.3)
+        t0.record(stream)
+        for i in range(args.steps):
+            lib = pg.load_library()
+            lib.pgb_fill_zero(step.grad.data_ptr(), step.grad.numel() * 4, stream.cuda_stream)
+            k_start[i].record(stream)
+            step.step_cameras(T, imgs, W["camera_angle_x"], R, 1000 * rank + args.warmup + i,
+                              near=W["near"], zero_grad=False)
+            k_end[i].record(stream)
+            if world > 1:
+                torch.distributed.all_reduce(step.grad)
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = pg.launch_count() - launches0
+    ms_total = t0.elapsed_time(t1)
+    kern_ms = sum(a.elapsed_time(b) for a, b in zip(k_start, k_end)) / args.steps
+    if world > 1:
+        tt = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(tt)
+        torch.distributed.barrier()
+    ms_step = ms_total / args.steps
+    value = world * R / (ms_step / 1e3)
+
+    # e2e: host ray batches through the public API (pinned H2D each step, loss D2H)
+    nb = 4
+    host = []
+    for b in range(nb):
+        dirs, pixels = pg.generate_rays_batched(imgs, R // W["cameras"] + 1, T, W["camera_angle_x"],
+                                                device=dev)
+        n = min(R, dirs.shape[0])
+        cam_pos = torch.repeat_interleave(T[:, :3, 3], R // W["cameras"] + 1, 0)
+        o = cam_pos + W["near"] * dirs
+        host.append(tuple(x[:n].cpu().pin_memory() for x in (o, dirs, pixels)))
+    dev_o = torch.empty(R, 3, device=dev)
+    dev_d = torch.empty(R, 3, device=dev)
+    dev_t = torch.empty(R, 4, device=dev)
+    loss_host = torch.empty(args.steps, dtype=torch.float32).pin_memory()
+    h2d = sum(x.numel() * x.element_size() for x in host[0])
+    for i in range(args.warmup):
+        ho, hd, ht = host[i % nb]
+        dev_o.copy_(ho, non_blocking=True); dev_d.copy_(hd, non_blocking=True); dev_t.copy_(ht, non_blocking=True)
+        step.step_rays(dev_o, dev_d, dev_t)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        ho, hd, ht = host[i % nb]
+        dev_o.copy_(ho, non_blocking=True); dev_d.copy_(hd, non_blocking=True); dev_t.copy_(ht, non_blocking=True)
+        loss = step.step_rays(dev_o, dev_d, dev_t)
+        if world > 1:
+            torch.distributed.all_reduce(step.grad)
+        loss_host[i].copy_(loss, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        tt = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(tt)
+    e2e = {"value": world * R / (e2e_ms / 1e3), "unit": "rays/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": 4, "ms_per_step": e2e_ms}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # roofline of the fused kernel: algorithmic bytes per launch / measured duration
+    U, inb_frac = unique_cells(pg, grid, T, imgs, W, 1000 * rank + args.warmup, delta, pd)
+    alg_bytes = U * 16 + U * 16 + R * 60
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / (kern_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "kernel": "render_kernel<trilinear,train>",
+                "kernel_ms": kern_ms, "unique_cells": U, "algorithmic_bytes": alg_bytes,
+                "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "issued_gather_bytes": int(R * S * inb_frac * 8 * 16),
+                "step_bytes": alg_bytes + grid.numel() * 4}
+    line = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": dict(W, l2="inputs larger than L2: 256 MiB grid read and 256 MiB gradient "
+                                 "zeroed + scattered every step, 1 GiB of target images",
+                           parallelism=f"dp{world}" if world > 1 else "single"),
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+            "clocks": clk.summary()}
+    if not args.no_baselines:
+        grid_cpu, T_cpu, imgs_cpu = grid.cpu(), T.cpu(), imgs.cpu()
+        line["torch_gpu_baseline"] = torch_gpu_rate(W, grid, T, imgs, dev)
+        line["cpu_baseline"] = cpu_reference_rate(W, grid_cpu, T_cpu, imgs_cpu)
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

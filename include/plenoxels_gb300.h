@@ -1,0 +1,214 @@
+/*
+ * plenoxels_gb300 — C ABI of the GB300 (sm_103a) differentiable voxel-grid renderer.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream, launches
+ * asynchronously on that stream, allocates nothing, and returns PGB_OK (0) or a
+ * negative PGB_ERR_* code for an argument or launch error. No entry point
+ * synchronises the device. Each entry point names the reference function it
+ * replaces (paths are relative to the DanJbk/Plenoxels repository).
+ *
+ * Grid layout (src/grid_functions.py:184-217 generate_grid): a dense, contiguous,
+ * channels-last [X, Y, Z, 4] tensor of interleaved R, G, B, alpha cells. Cell
+ * (i, j, k) sits at world position origin + (i, j, k) * points_distance, where
+ * origin is the per-axis minimum of the reference's grid coordinate table
+ * ((1 - ceil(s/2)) * points_distance).
+ *
+ * Storage types: PGB_F32 (16 B cells), PGB_BF16 (8 B cells, fp32 arithmetic and fp32
+ * gradients) and PGB_F64 (32 B cells, fp64 arithmetic; used for finite-difference
+ * checks). "Real" below means float for F32/BF16 grids and double for F64 grids.
+ */
+#ifndef PLENOXELS_GB300_H
+#define PLENOXELS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same object as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st* pgb_stream_t;
+
+enum {
+  PGB_OK = 0,
+  PGB_ERR_ARG = -1,         /* null pointer, bad size, bad enum */
+  PGB_ERR_ALIGN = -2,       /* a pointer is not aligned for vector cell access */
+  PGB_ERR_LAUNCH = -3,      /* the CUDA launch itself failed */
+  PGB_ERR_UNSUPPORTED = -4  /* valid but unsupported combination (e.g. too many samples) */
+};
+
+enum { PGB_F32 = 0, PGB_BF16 = 1, PGB_F64 = 2 };
+enum { PGB_NEAREST = 0, PGB_TRILINEAR = 1 };
+
+/* A dense channels-last RGBA voxel grid. */
+typedef struct {
+  const void* cells;        /* [X,Y,Z,4] of dtype; 16-byte aligned (8 for BF16) */
+  int32_t dtype;            /* PGB_F32 | PGB_BF16 | PGB_F64 */
+  int32_t dims[3];          /* X, Y, Z */
+  double origin[3];         /* world position of cell (0,0,0), held exactly in "Real" */
+  double points_distance;   /* cell pitch, held exactly in "Real" */
+  int32_t clip;             /* 1: clamp cell values to [0,1] at lookup (scripts/train.py:146) */
+  int32_t mode;             /* PGB_NEAREST | PGB_TRILINEAR */
+} pgb_grid;
+
+/* Cameras for in-kernel ray generation (src/ray_sampling.py:195-264). */
+typedef struct {
+  const float* transforms;  /* [C,4,4] camera-to-world; columns x, y, back, position */
+  const float* images;      /* [C,H,W,4] RGBA target pixels */
+  int32_t num_cameras;      /* C */
+  int32_t height, width;    /* H, W (square images only, as the reference indexes them) */
+  float camera_angle_x;     /* horizontal field of view, used linearly (ray_sampling.py:234) */
+  float near;               /* rays start at position + near * direction */
+  uint64_t seed;            /* pixel-position RNG seed (counter-based hash; see pgb_hash_uniform) */
+} pgb_cameras;
+
+/* A batch of rays and how each ray is sampled (src/ray_sampling.py:128-169). */
+typedef struct {
+  const void* origins;      /* [R,3] Real: first point of each ray (NULL when cameras != NULL) */
+  const void* dirs;         /* [R,3] Real: unit directions (NULL when cameras != NULL) */
+  const pgb_cameras* cameras; /* host pointer; non-NULL: rays generated in-kernel, camera-major */
+  int64_t num_rays;         /* R */
+  int32_t num_samples;      /* S: samples at t_k = delta_step * k, k = 1..S */
+  double delta_step;        /* held exactly in "Real" */
+  int32_t stratified;       /* 1: t_k = delta_step * (k - j_k), j_k in [0,1) from the hash */
+  uint64_t seed;            /* stratification seed */
+  float term_threshold;     /* >0: stop a ray once its transmittance falls below this */
+} pgb_rays;
+
+/* ---- fused render path (scripts/train.py:142-156 composed with src/ray_sampling.py,
+ *      src/grid_functions.py; one warp per ray, no per-sample intermediates) ---- */
+
+/* Forward: rgba_out[R,4] = composited premultiplied RGB and accumulated alpha.
+ * Replaces sample_camera_rays_batched -> normalize_samples_for_indecies ->
+ * get_nearest_voxels | trilinear_interpolation -> *mask -> compute_alpha_weighted_pixels
+ * (scripts/train.py:130-151). */
+int pgb_render_fwd(const pgb_grid* grid, const pgb_rays* rays, void* rgba_out, pgb_stream_t stream);
+
+/* Backward of pgb_render_fwd: accumulates dL/dcells into grad_cells ([X,Y,Z,4], fp32 for
+ * F32/BF16 grids, fp64 for F64), which the caller zeroes first. Replaces the autograd
+ * replay of loss.backward() (scripts/train.py:181). */
+int pgb_render_bwd(const pgb_grid* grid, const pgb_rays* rays, const void* d_rgba,
+                   void* grad_cells, pgb_stream_t stream);
+
+/* Fused training step: forward, MSE against target (mean over R*4 entries times
+ * loss_weight, scripts/train.py:156), and backward in one launch. target is [R,4] Real
+ * (ignored when rays->cameras is set: targets are the sampled image pixels).
+ * rgba_out may be NULL. loss_out[0] receives the loss (Real). workspace must hold
+ * pgb_train_workspace_bytes() bytes and be zeroed once before first use; the kernel
+ * leaves it zeroed again. */
+int pgb_render_train(const pgb_grid* grid, const pgb_rays* rays, const void* target,
+                     double loss_weight, void* rgba_out, void* grad_cells, void* loss_out,
+                     void* workspace, pgb_stream_t stream);
+int64_t pgb_train_workspace_bytes(void);
+
+/* Debug/parity view of the fused kernels' own index math: for every sample of every
+ * ray, the wrapped cell indices the lookup reads (nearest: [R,S,3]; trilinear:
+ * [R,S,8,3], corner order of src/grid_functions.py:16-24) and the in-bounds flag
+ * [R,S]. index_out is int64. */
+int pgb_render_sample_indices(const pgb_grid* grid, const pgb_rays* rays, int64_t* index_out,
+                              uint8_t* inbounds_out, pgb_stream_t stream);
+
+/* ---- drop-in operators, one per reference function ---- */
+
+/* src/ray_sampling.py:195-264 generate_rays_batched. uv: [C*Rc,2] uniforms in [0,1)
+ * (the reference's torch.rand draw), or NULL with even_spread=1 (linspace grid of
+ * side x side rays, side*side == Rc). Writes dirs_out[C*Rc,3], pixels_out[C*Rc,4].
+ * status_out (optional device int32) is OR-ed with 1 when a pixel index falls outside
+ * the image (the reference raises IndexError there); that ray's pixel is zero. */
+int pgb_generate_rays(const float* transforms, int32_t num_cameras, int64_t rays_per_camera,
+                      float camera_angle_x, const float* images, int32_t height, int32_t width,
+                      const float* uv, int32_t even_spread, float* dirs_out, float* pixels_out,
+                      int32_t* status_out, pgb_stream_t stream);
+
+/* src/ray_sampling.py:159-167: samples_out[C*Rc*S,3] = position(camera(r)) +
+ * dirs[r] * (delta_step * k), k = 1..S. transforms gives the camera positions. */
+int pgb_sample_points(const float* transforms, int32_t num_cameras, int64_t rays_per_camera,
+                      const float* dirs, int32_t num_samples, float delta_step,
+                      float* samples_out, pgb_stream_t stream);
+
+/* src/ray_sampling.py:13, the grid_indices.min(0) reduction: min_out[3] (device). */
+int pgb_coords_min(const float* coords, int64_t count, float* min_out, pgb_stream_t stream);
+
+/* src/ray_sampling.py:12-13 normalize_samples_for_indecies:
+ * out = (samples - grid_min) / points_distance with IEEE division. grid_min is device [3]. */
+int pgb_normalize_samples(const float* samples, int64_t count, const float* grid_min,
+                          float points_distance, float* out, pgb_stream_t stream);
+
+/* src/grid_functions.py:103-114 get_nearest_voxels (with :47-63 and :66-79):
+ * round half to even, in-bounds flag, periodic wrap, gather. normalized is [N,3] Real.
+ * vals_out [N,4] Real, inbounds_out [N] (0/1), index_out [N,3] int64 (optional). */
+int pgb_nearest_gather(const pgb_grid* grid, const void* normalized, int64_t count,
+                       void* vals_out, uint8_t* inbounds_out, int64_t* index_out,
+                       pgb_stream_t stream);
+/* Backward of pgb_nearest_gather: grad_cells[idx] += d_vals (clip mask applied). */
+int pgb_nearest_scatter(const pgb_grid* grid, const void* normalized, int64_t count,
+                        const void* d_vals, void* grad_cells, pgb_stream_t stream);
+
+/* src/grid_functions.py:184-217 generate_grid: world coordinates coords_out [X,Y,Z,3]
+ * fp32 = (index - ceil(dim/2) + 1) * points_distance and the integer index table
+ * meshgrid_out [X,Y,Z,3] int64 (either may be NULL). */
+int pgb_grid_coords(const int32_t dims[3], float points_distance, float* coords_out,
+                    int64_t* meshgrid_out, pgb_stream_t stream);
+
+/* src/grid_functions.py:154-170 (the gather of collect_cell_information_via_indices):
+ * vals_out[M,4] = cells[idx[m]] for int64 indices [M,3]. Negative indices count from the
+ * end; an index outside the grid OR-s 1 into status_out and yields zeros. */
+int pgb_gather_cells(const pgb_grid* grid, const int64_t* indices, int64_t count, void* vals_out,
+                     int32_t* status_out, pgb_stream_t stream);
+/* Backward of pgb_gather_cells: grad_cells[idx[m]] += d_vals[m] (clip mask applied). */
+int pgb_scatter_cells(const pgb_grid* grid, const int64_t* indices, int64_t count,
+                      const void* d_vals, void* grad_cells, int32_t* status_out,
+                      pgb_stream_t stream);
+
+/* src/grid_functions.py:220-246 get_grid_points_indices: corners_out [N,8,3] int64. */
+int pgb_corner_indices(const void* normalized, int32_t dtype, int64_t count,
+                       int64_t* corners_out, pgb_stream_t stream);
+
+/* src/grid_functions.py:47-63 find_out_of_bound on float or int64 indices [N,3]. */
+int pgb_in_bounds(const void* indices, int32_t index_kind, int64_t count, const int32_t dims[3],
+                  uint8_t* out, pgb_stream_t stream);
+enum { PGB_INDEX_F32 = 0, PGB_INDEX_F64 = 1, PGB_INDEX_I64 = 2 };
+
+/* src/grid_functions.py:66-79 fix_out_of_bounds: in-place floor-mod of [M,3] int64. */
+int pgb_wrap_indices(int64_t* indices, int64_t count, const int32_t dims[3], pgb_stream_t stream);
+
+/* src/grid_functions.py:7-44 trilinear_interpolation: out[N,4] Real from the already
+ * wrapped corners [N,8,3] int64 and frac(normalized). grid->clip applies the clamp.
+ * Negative corner indices count from the end (torch indexing); a corner outside the
+ * grid is skipped and OR-s 1 into status_out (optional device int32), where the
+ * reference raises IndexError. */
+int pgb_trilinear_gather(const pgb_grid* grid, const void* normalized, const int64_t* corners,
+                         int64_t count, void* out, int32_t* status_out, pgb_stream_t stream);
+/* Backward of pgb_trilinear_gather into grad_cells. */
+int pgb_trilinear_scatter(const pgb_grid* grid, const void* normalized, const int64_t* corners,
+                          int64_t count, const void* d_out, void* grad_cells,
+                          int32_t* status_out, pgb_stream_t stream);
+
+/* src/ray_sampling.py:172-192 compute_alpha_weighted_pixels over [M,S,4] samples
+ * (M = cameras * rays). out[M,4] = (sum w*rgb, sum w), w_k = a_k * prod_{j<k}(1 - a_j). */
+int pgb_composite_fwd(const void* samples, int32_t dtype, int64_t num_rays, int32_t num_samples,
+                      void* out, pgb_stream_t stream);
+/* Backward: d_samples[M,S,4] from d_out[M,4] (division-free, exact at alpha == 1). */
+int pgb_composite_bwd(const void* samples, int32_t dtype, int64_t num_rays, int32_t num_samples,
+                      const void* d_out, void* d_samples, pgb_stream_t stream);
+
+/* ---- utilities ---- */
+
+/* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel. */
+int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream);
+
+/* The counter-based uniform in [0,1) used for stratification and in-kernel ray
+ * generation, evaluated on the host: uniform(seed, a, b). Exact multiples of 2^-24. */
+float pgb_hash_uniform(uint64_t seed, uint64_t a, uint32_t b);
+
+/* Number of kernels this library has launched in this process (all entry points). */
+int64_t pgb_launch_count(void);
+
+const char* pgb_version(void);
+const char* pgb_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLENOXELS_GB300_H */

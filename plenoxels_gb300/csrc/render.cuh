@@ -1,0 +1,462 @@
+// Fused render kernels: ray sampling -> voxel lookup -> front-to-back compositing, and the
+// hand-written adjoint, one warp per ray.
+//
+// What one launch replaces (paths relative to the reference repository):
+//   src/ray_sampling.py:195-264  generate_rays_batched       (in-kernel when cameras are given)
+//   src/ray_sampling.py:161-167  sample positions o + d * (delta * k)
+//   src/ray_sampling.py:12-13    normalisation (p - min) / points_distance
+//   src/grid_functions.py:103-114 nearest lookup / :7-44, :220-246 trilinear lookup
+//   scripts/train.py:146-147     grid.clip(0, 1) and the in-bounds mask
+//   src/ray_sampling.py:172-192  compute_alpha_weighted_pixels
+//   scripts/train.py:156, 181    mse_loss and its backward through all of the above
+//
+// Work layout: a warp owns one ray at a time. Samples are dealt to lanes in "slots":
+// slot k of lane l is sample 32*k + l, so each load instruction of a warp touches 32
+// consecutive samples of one ray (a compact run of cells). A chunk is K slots (32*K
+// samples). The transmittance is an exclusive prefix product, computed per slot with a
+// warp scan and carried across slots and chunks. The adjoint needs, per sample,
+//     d alpha_s = T_s * (G_s - S_{s+1}),   G_s = <g_rgb, c_s> + g_A,
+//     S_s = G_s * alpha_s + (1 - alpha_s) * S_{s+1},  S_{end} = 0,
+// a suffix recurrence of affine maps evaluated with a second warp scan. It contains no
+// division, so alpha == 1 (transmittance exactly 0 after the clip) is exact. Per-sample
+// values stay in registers; with more than one chunk the earlier chunks are re-gathered
+// in the reverse pass (the transmittance at each chunk start is kept in lane c).
+#pragma once
+
+#include "pgb_device.cuh"
+
+namespace pgb {
+
+enum Phase { kForward = 0, kBackward = 1, kTrain = 2 };
+
+template <typename Real>
+struct GridP {
+  const void* cells;
+  int X, Y, Z;
+  Real fX, fY, fZ;
+  Real ox, oy, oz;
+  Real pd;
+  int clip;
+};
+
+template <typename Real>
+struct RenderArgs {
+  GridP<Real> g;
+  // explicit rays
+  const Real* origins;
+  const Real* dirs;
+  // in-kernel camera rays
+  int use_cameras;
+  const float* transforms;
+  const float* images;
+  int C, H, W;
+  float fov, near_dist;
+  uint64_t cam_seed;
+  // sampling
+  int64_t R;
+  int S;
+  Real delta;
+  int stratified;
+  uint64_t strat_seed;
+  float term_thr;
+  // outputs / adjoint inputs
+  Real* rgba_out;
+  const Real* d_rgba;
+  const Real* target;
+  Real* grad;
+  Real* loss_out;
+  double* partials;
+  unsigned* counter;
+  double loss_w;
+  double inv_count;
+};
+
+template <typename Real>
+struct Ray {
+  Real ox, oy, oz, dx, dy, dz;
+  Real tgt[4];
+  uint64_t h;  // stratification stream of this ray
+};
+
+// Euclidean norm as the reference's CPU torch.norm evaluates a 3-vector:
+// sqrt(fma(z, z, fma(y, y, x * x))).
+__device__ __forceinline__ float norm3_ref(float x, float y, float z) {
+  return rsqrt_exact(rfma(z, z, rfma(y, y, rmul(x, x))));
+}
+
+// Direction of a camera ray from uniforms (u, v), src/ray_sampling.py:215-262, rounded
+// op by op as the reference's fp32 tensor program.
+__device__ __forceinline__ void camera_direction(const float* T, float fov, float u, float v,
+                                                 float d[3]) {
+  // T is row-major 4x4: column 0 = x axis, column 1 = y axis, column 2 = back axis.
+  const float xa0 = T[0], xa1 = T[4], xa2 = T[8];
+  const float ya0 = T[1], ya1 = T[5], ya2 = T[9];
+  const float za0 = -T[2], za1 = -T[6], za2 = -T[10];
+  const float aspect = rdiv(norm3_ref(xa0, xa1, xa2), norm3_ref(ya0, ya1, ya2));
+  const float ru = rmul(fov, rsub(u, 0.5f));
+  const float rv = -rmul(rmul(fov, rdiv(1.0f, aspect)), rsub(v, 0.5f));
+  const float e0 = radd(radd(rmul(ru, xa0), rmul(rv, ya0)), za0);
+  const float e1 = radd(radd(rmul(ru, xa1), rmul(rv, ya1)), za1);
+  const float e2 = radd(radd(rmul(ru, xa2), rmul(rv, ya2)), za2);
+  const float n = norm3_ref(e0, e1, e2);
+  d[0] = rdiv(e0, n);
+  d[1] = rdiv(e1, n);
+  d[2] = rdiv(e2, n);
+}
+
+// Pixel of a ray (src/ray_sampling.py:238-248): column from u scaled by H, row from v
+// scaled by W, round half to even, clamp to the last index.
+__device__ __forceinline__ void camera_pixel(int H, int W, float u, float v, int& row, int& col) {
+  col = (int)fminf(rintf(rmul((float)H, u)), (float)(H - 1));
+  row = (int)fminf(rintf(rmul((float)W, v)), (float)(W - 1));
+}
+
+template <typename Real>
+__device__ __forceinline__ void load_ray(const RenderArgs<Real>& a, int64_t r, Ray<Real>& ray,
+                                         bool need_target) {
+  if (a.use_cameras) {
+    // cameras get contiguous runs of rays (camera-major, src/ray_sampling.py:243)
+    const int c = (int)((r * (int64_t)a.C) / a.R);
+    const float* T = a.transforms + 16 * (int64_t)c;
+    const uint64_t h = hash_stream(a.cam_seed, (uint64_t)r);
+    const float u = hash_to_unit(h, 0u), v = hash_to_unit(h, 1u);
+    float d[3];
+    camera_direction(T, a.fov, u, v, d);
+    ray.dx = d[0]; ray.dy = d[1]; ray.dz = d[2];
+    ray.ox = radd(T[3], rmul(a.near_dist, d[0]));
+    ray.oy = radd(T[7], rmul(a.near_dist, d[1]));
+    ray.oz = radd(T[11], rmul(a.near_dist, d[2]));
+    if (need_target) {
+      int row, col;
+      camera_pixel(a.H, a.W, u, v, row, col);
+      const float4 px = __ldg(reinterpret_cast<const float4*>(a.images) +
+                              (((int64_t)c * a.H + row) * a.W + col));
+      ray.tgt[0] = px.x; ray.tgt[1] = px.y; ray.tgt[2] = px.z; ray.tgt[3] = px.w;
+    }
+  } else {
+    ray.ox = a.origins[3 * r + 0]; ray.oy = a.origins[3 * r + 1]; ray.oz = a.origins[3 * r + 2];
+    ray.dx = a.dirs[3 * r + 0];    ray.dy = a.dirs[3 * r + 1];    ray.dz = a.dirs[3 * r + 2];
+    if (need_target) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) ray.tgt[c] = a.target[4 * r + c];
+    }
+  }
+  ray.h = a.stratified ? hash_stream(a.strat_seed, (uint64_t)r) : 0ull;
+}
+
+// Normalised grid coordinates of sample s (0-based) of a ray:
+//   t = delta * (s + 1) [- jitter],  p = o + d * t,  n = (p - origin) / pd
+// each op rounded separately (src/ray_sampling.py:161-167, :13).
+template <typename Real>
+__device__ __forceinline__ void sample_coords(const RenderArgs<Real>& a, const Ray<Real>& ray,
+                                              int s, Real& nx, Real& ny, Real& nz) {
+  Real k = (Real)(s + 1);
+  if (a.stratified) k = rsub(k, (Real)hash_to_unit(ray.h, (uint32_t)s));
+  const Real t = rmul(a.delta, k);
+  const Real px = radd(ray.ox, rmul(ray.dx, t));
+  const Real py = radd(ray.oy, rmul(ray.dy, t));
+  const Real pz = radd(ray.oz, rmul(ray.dz, t));
+  nx = rdiv(rsub(px, a.g.ox), a.g.pd);
+  ny = rdiv(rsub(py, a.g.oy), a.g.pd);
+  nz = rdiv(rsub(pz, a.g.oz), a.g.pd);
+}
+
+template <typename Real>
+__device__ __forceinline__ uint64_t cell_index(const GridP<Real>& g, int i, int j, int k) {
+  return ((uint64_t)i * (uint64_t)g.Y + (uint64_t)j) * (uint64_t)g.Z + (uint64_t)k;
+}
+
+// Trilinear corner geometry of an in-bounds sample: wrapped ceil/floor indices per axis
+// and the fractional weights (src/grid_functions.py:29, :230-244, :75-77). For an
+// in-bounds coordinate 0 <= n < dim, only ceil can leave the grid (n in (dim-1, dim)),
+// and it wraps to 0.
+template <typename Real>
+struct Corners {
+  int c[3], f[3];
+  Real w[3];  // frac(n) per axis
+};
+
+template <typename Real>
+__device__ __forceinline__ bool trilinear_corners(const GridP<Real>& g, Real nx, Real ny, Real nz,
+                                                  Corners<Real>& q) {
+  if (!(nx >= Real(0) && nx < g.fX && ny >= Real(0) && ny < g.fY && nz >= Real(0) && nz < g.fZ))
+    return false;
+  const Real n[3] = {nx, ny, nz};
+  const int dim[3] = {g.X, g.Y, g.Z};
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    const Real fl = rfloor(n[ax]);
+    q.f[ax] = (int)fl;
+    const int ce = (int)rceil(n[ax]);
+    q.c[ax] = ce >= dim[ax] ? ce - dim[ax] : ce;
+    q.w[ax] = rsub(n[ax], fl);  // == n - trunc(n) for n >= 0
+  }
+  return true;
+}
+
+// Value of one sample, masked to zero outside the grid. bits: gradient-pass flags of
+// the clamp, bit 4*corner + channel (trilinear; corner order of
+// src/grid_functions.py:16-24) or bit channel (nearest). Zero when out of bounds.
+template <typename Real, typename Store, int MODE>
+__device__ __forceinline__ void sample_value(const GridP<Real>& g, Real nx, Real ny, Real nz,
+                                             Real v[4], uint32_t& bits) {
+  bits = 0u;
+  v[0] = v[1] = v[2] = v[3] = Real(0);
+  if (MODE == PGB_NEAREST) {
+    const Real rx = rround(nx), ry = rround(ny), rz = rround(nz);
+    if (!(rx >= Real(0) && rx < g.fX && ry >= Real(0) && ry < g.fY && rz >= Real(0) && rz < g.fZ))
+      return;
+    Real cv[4];
+    CellIO<Store>::load(g.cells, cell_index(g, (int)rx, (int)ry, (int)rz), cv);
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+      if (g.clip) {
+        bits |= (in01(cv[ch]) ? 1u : 0u) << ch;
+        v[ch] = clamp01(cv[ch]);
+      } else {
+        bits |= 1u << ch;
+        v[ch] = cv[ch];
+      }
+    }
+  } else {
+    Corners<Real> q;
+    if (!trilinear_corners(g, nx, ny, nz, q)) return;
+    Real cv[8][4];
+#pragma unroll
+    for (int corner = 0; corner < 8; ++corner) {
+      const int ix = (corner & 4) ? q.f[0] : q.c[0];
+      const int iy = (corner & 2) ? q.f[1] : q.c[1];
+      const int iz = (corner & 1) ? q.f[2] : q.c[2];
+      CellIO<Store>::load(g.cells, cell_index(g, ix, iy, iz), cv[corner]);
+    }
+#pragma unroll
+    for (int corner = 0; corner < 8; ++corner) {
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        if (g.clip) {
+          bits |= (in01(cv[corner][ch]) ? 1u : 0u) << (4 * corner + ch);
+          cv[corner][ch] = clamp01(cv[corner][ch]);
+        } else {
+          bits |= 1u << (4 * corner + ch);
+        }
+      }
+    }
+    // blend x, then y, then z, as src/grid_functions.py:34-42
+    const Real wx = q.w[0], wy = q.w[1], wz = q.w[2];
+    const Real ux = rsub(Real(1), wx), uy = rsub(Real(1), wy), uz = rsub(Real(1), wz);
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+      Real a4[4];
+#pragma unroll
+      for (int yz = 0; yz < 4; ++yz)
+        a4[yz] = radd(rmul(cv[yz][ch], wx), rmul(cv[4 + yz][ch], ux));
+      const Real b0 = radd(rmul(a4[0], wy), rmul(a4[2], uy));
+      const Real b1 = radd(rmul(a4[1], wy), rmul(a4[3], uy));
+      v[ch] = radd(rmul(b0, wz), rmul(b1, uz));
+    }
+  }
+}
+
+// Scatter dL/dvalue of one sample into the dense gradient (the autograd replay of the
+// blend, the clamp mask and index_put accumulate).
+template <typename Real, int MODE>
+__device__ __forceinline__ void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, Real ny,
+                                               Real nz, const Real dv[4], uint32_t bits) {
+  if (bits == 0u) return;
+  if (MODE == PGB_NEAREST) {
+    Real gv[4];
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) gv[ch] = ((bits >> ch) & 1u) ? dv[ch] : Real(0);
+    const uint64_t c = cell_index(g, (int)rround(nx), (int)rround(ny), (int)rround(nz));
+    grad_add(grad, c, gv);
+  } else {
+    Corners<Real> q;
+    trilinear_corners(g, nx, ny, nz, q);
+    const Real wx = q.w[0], wy = q.w[1], wz = q.w[2];
+    const Real ux = rsub(Real(1), wx), uy = rsub(Real(1), wy), uz = rsub(Real(1), wz);
+#pragma unroll
+    for (int corner = 0; corner < 8; ++corner) {
+      const Real sz = (corner & 1) ? uz : wz;
+      const Real sy = (corner & 2) ? uy : wy;
+      const Real sx = (corner & 4) ? ux : wx;
+      Real gv[4];
+      bool any = false;
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        const Real t = rmul(rmul(rmul(dv[ch], sz), sy), sx);
+        gv[ch] = ((bits >> (4 * corner + ch)) & 1u) ? t : Real(0);
+        any |= gv[ch] != Real(0);
+      }
+      if (any) {
+        const int ix = (corner & 4) ? q.f[0] : q.c[0];
+        const int iy = (corner & 2) ? q.f[1] : q.c[1];
+        const int iz = (corner & 1) ? q.f[2] : q.c[2];
+        grad_add(grad, cell_index(g, ix, iy, iz), gv);
+      }
+    }
+  }
+}
+
+// Gathers chunk `c` (K slots) of a ray into registers.
+template <typename Real, typename Store, int MODE, int K>
+__device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ray<Real>& ray, int c,
+                                             int lane, Real v[K][4], uint32_t bits[K]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int s = (c * K + k) * kWarp + lane;
+    if (s < a.S) {
+      Real nx, ny, nz;
+      sample_coords(a, ray, s, nx, ny, nz);
+      sample_value<Real, Store, MODE>(a.g, nx, ny, nz, v[k], bits[k]);
+    } else {
+      v[k][0] = v[k][1] = v[k][2] = v[k][3] = Real(0);
+      bits[k] = 0u;
+    }
+  }
+}
+
+// Exclusive transmittance of every sample of a chunk from the chunk's starting T;
+// returns T after the chunk.
+template <typename Real, int K>
+__device__ __forceinline__ Real scan_chunk(const Real v[K][4], Real T, int lane, Real Ts[K]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const Real incl = warp_incl_prod(Real(1) - v[k][3], lane);
+    Real excl = __shfl_up_sync(kFull, incl, 1);
+    if (lane == 0) excl = Real(1);
+    Ts[k] = T * excl;
+    T *= __shfl_sync(kFull, incl, kWarp - 1);
+  }
+  return T;
+}
+
+// v[i] for a runtime i in [0,4) without indexing a register array dynamically.
+template <typename Real>
+__device__ __forceinline__ Real pick4(const Real v[4], int i) {
+  return i == 0 ? v[0] : (i == 1 ? v[1] : (i == 2 ? v[2] : v[3]));
+}
+
+template <typename Real, typename Store, int MODE, int K, int PHASE>
+__global__ void __launch_bounds__(256) render_kernel(const RenderArgs<Real> a) {
+  const int lane = threadIdx.x & (kWarp - 1);
+  const int warps_per_block = blockDim.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const int64_t nw = (int64_t)gridDim.x * warps_per_block;
+  const int nchunks = (a.S + kWarp * K - 1) / (kWarp * K);
+  double loss_lane = 0.0;
+
+  for (int64_t r = gw; r < a.R; r += nw) {
+    Ray<Real> ray;
+    load_ray(a, r, ray, PHASE == kTrain);
+
+    Real v[K][4];
+    uint32_t bits[K];
+    Real Ts[K];
+    Real acc[4] = {Real(0), Real(0), Real(0), Real(0)};
+    Real T = Real(1);
+    Real Tstart = Real(1);  // lane c: transmittance at the start of chunk c
+    int last = 0;
+    for (int c = 0; c < nchunks; ++c) {
+      if (lane == c) Tstart = T;
+      gather_chunk<Real, Store, MODE, K>(a, ray, c, lane, v, bits);
+      T = scan_chunk<Real, K>(v, T, lane, Ts);
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const Real w = v[k][3] * Ts[k];
+        acc[0] += w * v[k][0];
+        acc[1] += w * v[k][1];
+        acc[2] += w * v[k][2];
+        acc[3] += w;
+      }
+      last = c;
+      if (a.term_thr > 0.0f && T < (Real)a.term_thr) break;
+    }
+    Real px[4];
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) px[ch] = warp_sum(acc[ch]);
+
+    if (PHASE == kForward) {
+      if (lane < 4) a.rgba_out[4 * r + lane] = pick4(px, lane);
+      continue;
+    }
+
+    Real gpx[4];
+    if (PHASE == kBackward) {
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) gpx[ch] = a.d_rgba[4 * r + ch];
+    } else {
+      double sq = 0.0;
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        const Real diff = px[ch] - ray.tgt[ch];
+        sq += (double)diff * (double)diff;
+        gpx[ch] = (Real)(2.0 * a.loss_w * a.inv_count) * diff;
+      }
+      if (lane == 0) loss_lane += sq;
+      if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = pick4(px, lane);
+    }
+
+    // reverse pass over the chunks that were composited
+    Real Snext_carry = Real(0);  // S at the first sample after the current chunk
+    for (int c = last; c >= 0; --c) {
+      if (c != last) {
+        gather_chunk<Real, Store, MODE, K>(a, ray, c, lane, v, bits);
+        scan_chunk<Real, K>(v, __shfl_sync(kFull, Tstart, c), lane, Ts);
+      }
+#pragma unroll
+      for (int k = K - 1; k >= 0; --k) {
+        const Real al = v[k][3];
+        const Real G = gpx[0] * v[k][0] + gpx[1] * v[k][1] + gpx[2] * v[k][2] + gpx[3];
+        Real fa = G * al, fb = Real(1) - al;
+        warp_suffix_affine(fa, fb, lane);
+        const Real S_here = fa + fb * Snext_carry;      // S_s for this lane's sample
+        Real S_after = __shfl_down_sync(kFull, S_here, 1);  // S_{s+1}
+        if (lane == kWarp - 1) S_after = Snext_carry;
+        Snext_carry = __shfl_sync(kFull, S_here, 0);
+        const int s = (c * K + k) * kWarp + lane;
+        if (bits[k] != 0u && s < a.S) {
+          const Real w = al * Ts[k];
+          Real dv[4];
+          dv[0] = gpx[0] * w;
+          dv[1] = gpx[1] * w;
+          dv[2] = gpx[2] * w;
+          dv[3] = Ts[k] * (G - S_after);
+          Real nx, ny, nz;
+          sample_coords(a, ray, s, nx, ny, nz);
+          sample_scatter<Real, MODE>(a.g, a.grad, nx, ny, nz, dv, bits[k]);
+        }
+      }
+    }
+  }
+
+  if (PHASE == kTrain) {
+    // deterministic loss: fixed-order block sum, then the last block sums the blocks
+    __shared__ double red[32];
+    __shared__ bool is_last;
+    const int wib = threadIdx.x >> 5;
+    if (lane == 0) red[wib] = loss_lane;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int i = 0; i < warps_per_block; ++i) s += red[i];
+      a.partials[blockIdx.x] = s;
+      __threadfence();
+      const unsigned done = atomicAdd(a.counter, 1u);
+      is_last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (is_last && wib == 0) {
+      __threadfence();
+      double s = 0.0;
+      for (unsigned i = lane; i < gridDim.x; i += kWarp)
+        s += *((volatile double*)a.partials + i);
+      s = warp_sum(s);
+      if (lane == 0) {
+        a.loss_out[0] = (Real)(a.loss_w * s * a.inv_count);
+        *a.counter = 0u;
+      }
+    }
+  }
+}
+
+}  // namespace pgb

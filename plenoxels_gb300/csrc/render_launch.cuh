@@ -1,0 +1,49 @@
+// Compile-time dispatch of the fused render kernel over lookup mode, phase and slots per
+// lane. Included once per storage type (render_f32.cu, render_bf16.cu, render_f64.cu) so
+// the instantiations compile in parallel.
+#pragma once
+
+#include <algorithm>
+
+#include "pgb_host.h"
+#include "render.cuh"
+
+namespace pgb {
+
+template <typename Real, typename Store, int MODE, int K, int PHASE>
+int launch_render_k(const RenderArgs<Real>& a, cudaStream_t s) {
+  constexpr int kThreads = 256;
+  constexpr int kWarpsPerBlock = kThreads / kWarp;
+  int64_t blocks = (a.R + kWarpsPerBlock - 1) / kWarpsPerBlock;
+  blocks = std::min<int64_t>(blocks, PHASE == kTrain ? kMaxTrainBlocks : (int64_t)1 << 20);
+  if (blocks < 1) blocks = 1;
+  render_kernel<Real, Store, MODE, K, PHASE><<<(unsigned)blocks, kThreads, 0, s>>>(a);
+  return after_launch();
+}
+
+template <typename Real, typename Store, int MODE, int PHASE>
+int launch_render_mp(const RenderArgs<Real>& a, cudaStream_t s) {
+  switch (pick_slots(a.S)) {
+    case 2: return launch_render_k<Real, Store, MODE, 2, PHASE>(a, s);
+    case 4: return launch_render_k<Real, Store, MODE, 4, PHASE>(a, s);
+    case 8: return launch_render_k<Real, Store, MODE, 8, PHASE>(a, s);
+    case 16: return launch_render_k<Real, Store, MODE, 16, PHASE>(a, s);
+    default: return PGB_ERR_UNSUPPORTED;
+  }
+}
+
+template <typename Real, typename Store>
+int launch_render_t(const RenderArgs<Real>& a, int mode, int phase, cudaStream_t s) {
+  if (mode == PGB_NEAREST) {
+    if (phase == kForward) return launch_render_mp<Real, Store, PGB_NEAREST, kForward>(a, s);
+    if (phase == kBackward) return launch_render_mp<Real, Store, PGB_NEAREST, kBackward>(a, s);
+    if (phase == kTrain) return launch_render_mp<Real, Store, PGB_NEAREST, kTrain>(a, s);
+  } else if (mode == PGB_TRILINEAR) {
+    if (phase == kForward) return launch_render_mp<Real, Store, PGB_TRILINEAR, kForward>(a, s);
+    if (phase == kBackward) return launch_render_mp<Real, Store, PGB_TRILINEAR, kBackward>(a, s);
+    if (phase == kTrain) return launch_render_mp<Real, Store, PGB_TRILINEAR, kTrain>(a, s);
+  }
+  return PGB_ERR_ARG;
+}
+
+}  // namespace pgb

@@ -1,0 +1,232 @@
+"""Fused render path: one kernel per pass over a batch of rays.
+
+``render_rays`` is the whole of scripts/train.py:130-151 (ray samples -> normalisation
+-> clamp -> nearest or trilinear lookup -> in-bounds mask -> compositing) as one
+``torch.autograd.Function`` whose backward is the hand-written adjoint kernel.
+``FusedTrainStep`` adds the MSE loss of scripts/train.py:156 and the backward of
+:181 into the same launch, writing the dense grid gradient directly (no autograd graph),
+optionally generating the rays in-kernel from cameras and images.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import PgbCameras, PgbRays, check, ptr, require_cuda, stream_of
+from .grid_functions import grid_origin
+
+MODES = {"nearest": _lib.PGB_NEAREST, "trilinear": _lib.PGB_TRILINEAR}
+
+
+def _mode(mode) -> int:
+    if mode not in MODES:
+        raise ValueError(f"mode must be 'nearest' or 'trilinear', got {mode!r}")
+    return MODES[mode]
+
+
+def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, seed, term_threshold,
+               cameras=None) -> PgbRays:
+    r = PgbRays()
+    r.origins = ptr(origins)
+    r.dirs = ptr(dirs)
+    r.cameras = ctypes.pointer(cameras) if cameras is not None else None
+    r.num_rays = int(num_rays)
+    r.num_samples = int(num_samples)
+    r.delta_step = float(delta_step)
+    r.stratified = 1 if stratified else 0
+    r.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    r.term_threshold = float(term_threshold)
+    return r
+
+
+def _check_rays(grid, origins, dirs):
+    real = _lib.real_dtype(grid.dtype)
+    for name, t in (("origins", origins), ("dirs", dirs)):
+        if t.dim() != 2 or t.shape[1] != 3:
+            raise ValueError(f"{name} must be [R,3], got {tuple(t.shape)}")
+        if t.dtype != real:
+            raise TypeError(f"{name} must be {real} for a {grid.dtype} grid, got {t.dtype}")
+    if origins.shape[0] != dirs.shape[0]:
+        raise ValueError("origins and dirs must have the same number of rays")
+
+
+class _RenderRays(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, grid, origins, dirs, cfg):
+        lib = _lib.load()
+        R = origins.shape[0]
+        rgba = torch.empty(R, 4, dtype=_lib.real_dtype(grid.dtype), device=grid.device)
+        gdesc = _lib.make_grid(grid, cfg["origin"], cfg["points_distance"], cfg["mode"], cfg["clip"])
+        rdesc = _rays_desc(origins, dirs, R, cfg["num_samples"], cfg["delta_step"],
+                           cfg["stratified"], cfg["seed"], cfg["term_threshold"])
+        check(lib.pgb_render_fwd(gdesc, rdesc, ptr(rgba), stream_of(grid)), "render_rays")
+        ctx.save_for_backward(grid, origins, dirs)
+        ctx.cfg = cfg
+        return rgba
+
+    @staticmethod
+    def backward(ctx, d_rgba):
+        grid, origins, dirs = ctx.saved_tensors
+        cfg = ctx.cfg
+        lib = _lib.load()
+        s = stream_of(grid)
+        grad = torch.empty(grid.shape, dtype=_lib.real_dtype(grid.dtype), device=grid.device)
+        check(lib.pgb_fill_zero(ptr(grad), grad.numel() * grad.element_size(), s), "backward")
+        d_rgba = d_rgba.to(grad.dtype).contiguous()
+        gdesc = _lib.make_grid(grid, cfg["origin"], cfg["points_distance"], cfg["mode"], cfg["clip"])
+        rdesc = _rays_desc(origins, dirs, origins.shape[0], cfg["num_samples"], cfg["delta_step"],
+                           cfg["stratified"], cfg["seed"], cfg["term_threshold"])
+        check(lib.pgb_render_bwd(gdesc, rdesc, ptr(d_rgba), ptr(grad), s), "render_rays backward")
+        return grad, None, None, None
+
+
+def render_rays(grid, origins, dirs, delta_step, num_samples, points_distance, grid_min=None,
+                mode="trilinear", clip=True, stratified=False, seed=0, term_threshold=0.0):
+    """Premultiplied RGBA [R,4] of rays through a dense [X,Y,Z,4] grid.
+
+    Samples sit at origins + dirs * (delta_step * k), k = 1..num_samples (minus a
+    per-sample jitter in [0,1) when stratified); grid_min is the world position of cell
+    (0,0,0) (default: generate_grid's layout, grid_origin()). Differentiable in grid."""
+    require_cuda(grid, origins, dirs)
+    _check_rays(grid, origins, dirs)
+    if grid_min is None:
+        grid_min = grid_origin(grid.shape, points_distance, _lib.real_dtype(grid.dtype))
+    cfg = dict(origin=tuple(float(x) for x in grid_min), points_distance=float(points_distance),
+               mode=_mode(mode), clip=bool(clip), num_samples=int(num_samples),
+               delta_step=float(delta_step), stratified=bool(stratified), seed=int(seed),
+               term_threshold=float(term_threshold))
+    return _RenderRays.apply(grid.contiguous(), origins.contiguous(), dirs.contiguous(), cfg)
+
+
+def render_sample_indices(grid, origins, dirs, delta_step, num_samples, points_distance,
+                          grid_min=None, mode="trilinear", stratified=False, seed=0):
+    """The cell indices the fused kernels read, per sample: int64 [R,S,3] (nearest) or
+    [R,S,8,3] (trilinear), wrapped, and the in-bounds flags [R,S]."""
+    require_cuda(grid, origins, dirs)
+    _check_rays(grid, origins, dirs)
+    if grid_min is None:
+        grid_min = grid_origin(grid.shape, points_distance, _lib.real_dtype(grid.dtype))
+    R, S = origins.shape[0], int(num_samples)
+    m = _mode(mode)
+    shape = (R, S, 3) if m == _lib.PGB_NEAREST else (R, S, 8, 3)
+    idx = torch.empty(shape, dtype=torch.int64, device=grid.device)
+    inb = torch.empty(R, S, dtype=torch.bool, device=grid.device)
+    gdesc = _lib.make_grid(grid.contiguous(), grid_min, points_distance, m, True)
+    rdesc = _rays_desc(origins.contiguous(), dirs.contiguous(), R, S, delta_step, stratified, seed, 0.0)
+    check(_lib.load().pgb_render_sample_indices(gdesc, rdesc, ptr(idx), ptr(inb), stream_of(grid)),
+          "render_sample_indices")
+    return idx, inb
+
+
+def _camera_desc(transforms, images, camera_angle_x, ray_seed, near) -> PgbCameras:
+    require_cuda(transforms, images)
+    if transforms.dtype != torch.float32 or images.dtype != torch.float32:
+        raise TypeError("transforms and images must be float32")
+    if not (transforms.is_contiguous() and images.is_contiguous()):
+        raise ValueError("transforms and images must be contiguous")
+    if images.dim() != 4 or images.shape[-1] != 4 or transforms.shape[1:] != (4, 4):
+        raise ValueError("transforms must be [C,4,4] and images [C,H,W,4]")
+    cams = PgbCameras()
+    cams.transforms = ptr(transforms)
+    cams.images = ptr(images)
+    cams.num_cameras = transforms.shape[0]
+    cams.height, cams.width = images.shape[1], images.shape[2]
+    cams.camera_angle_x = float(camera_angle_x)
+    cams.near = float(near)
+    cams.seed = int(ray_seed) & 0xFFFFFFFFFFFFFFFF
+    return cams
+
+
+def camera_sample_indices(grid, transforms, images, camera_angle_x, num_rays, ray_seed, near,
+                          delta_step, num_samples, points_distance, grid_min=None,
+                          mode="trilinear", stratified=False, seed=0):
+    """render_sample_indices for rays generated in-kernel from cameras (the rays
+    FusedTrainStep.step_cameras uses for the same arguments)."""
+    require_cuda(grid)
+    if grid_min is None:
+        grid_min = grid_origin(grid.shape, points_distance, _lib.real_dtype(grid.dtype))
+    R, S = int(num_rays), int(num_samples)
+    m = _mode(mode)
+    shape = (R, S, 3) if m == _lib.PGB_NEAREST else (R, S, 8, 3)
+    idx = torch.empty(shape, dtype=torch.int64, device=grid.device)
+    inb = torch.empty(R, S, dtype=torch.bool, device=grid.device)
+    cams = _camera_desc(transforms, images, camera_angle_x, ray_seed, near)
+    gdesc = _lib.make_grid(grid.contiguous(), grid_min, points_distance, m, True)
+    rdesc = _rays_desc(None, None, R, S, delta_step, stratified, seed, 0.0, cameras=cams)
+    check(_lib.load().pgb_render_sample_indices(gdesc, rdesc, ptr(idx), ptr(inb), stream_of(grid)),
+          "camera_sample_indices")
+    return idx, inb
+
+
+class FusedTrainStep:
+    """Forward, MSE loss and backward of a batch of rays in one kernel launch.
+
+    The gradient goes to ``self.grad`` (fp32 for fp32/bf16 grids, fp64 for fp64 grids),
+    which is also attached as ``grid.grad`` when the dtypes agree, so a torch optimizer
+    can step on it. Each call zeroes the gradient first (optimizer.zero_grad semantics)
+    unless zero_grad=False, in which case it accumulates like autograd does. Every call
+    is asynchronous; the returned loss is a device scalar.
+    """
+
+    def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
+                 grid_min=None, clip=True, stratified=False, seed=0, term_threshold=0.0,
+                 loss_weight=1.0):
+        require_cuda(grid)
+        if grid.dim() != 4 or grid.shape[-1] != 4 or not grid.is_contiguous():
+            raise ValueError("grid must be a contiguous [X,Y,Z,4] tensor")
+        self.grid = grid
+        self.real = _lib.real_dtype(grid.dtype)
+        self.points_distance = float(points_distance)
+        self.grid_min = tuple(grid_min) if grid_min is not None else grid_origin(
+            grid.shape, points_distance, self.real)
+        self.num_samples = int(num_samples)
+        self.delta_step = float(delta_step)
+        self.mode = _mode(mode)
+        self.clip = bool(clip)
+        self.stratified = bool(stratified)
+        self.seed = int(seed)
+        self.term_threshold = float(term_threshold)
+        self.loss_weight = float(loss_weight)
+        lib = _lib.load()
+        dev = grid.device
+        self.workspace = torch.zeros(lib.pgb_train_workspace_bytes(), dtype=torch.uint8, device=dev)
+        self.grad = torch.zeros(grid.shape, dtype=self.real, device=dev)
+        self.loss = torch.zeros((), dtype=self.real, device=dev)
+        if grid.dtype == self.real and grid.requires_grad:
+            grid.grad = self.grad
+        self._cams = None
+
+    def _launch(self, rdesc, target, rgba_out, zero_grad):
+        lib = _lib.load()
+        s = stream_of(self.grid)
+        if zero_grad:
+            check(lib.pgb_fill_zero(ptr(self.grad), self.grad.numel() * self.grad.element_size(), s),
+                  "train step")
+        gdesc = _lib.make_grid(self.grid, self.grid_min, self.points_distance, self.mode, self.clip)
+        check(lib.pgb_render_train(gdesc, rdesc, ptr(target), self.loss_weight, ptr(rgba_out),
+                                   ptr(self.grad), ptr(self.loss), ptr(self.workspace), s),
+              "train step")
+        return self.loss
+
+    def step_rays(self, origins, dirs, target, rgba_out=None, zero_grad=True):
+        """Explicit rays [R,3] and their target pixels [R,4]."""
+        require_cuda(origins, dirs, target)
+        _check_rays(self.grid, origins, dirs)
+        if target.shape != (origins.shape[0], 4) or target.dtype != self.real:
+            raise ValueError(f"target must be [R,4] {self.real}")
+        rdesc = _rays_desc(origins, dirs, origins.shape[0], self.num_samples, self.delta_step,
+                           self.stratified, self.seed, self.term_threshold)
+        return self._launch(rdesc, target.contiguous(), rgba_out, zero_grad)
+
+    def step_cameras(self, transforms, images, camera_angle_x, num_rays, ray_seed, near=0.0,
+                     rgba_out=None, zero_grad=True):
+        """Rays generated in-kernel: num_rays spread camera-major over the cameras, pixel
+        positions from the counter hash of ray_seed, origins moved `near` along each ray;
+        targets are the sampled pixels of images [C,H,W,4]."""
+        cams = _camera_desc(transforms, images, camera_angle_x, ray_seed, near)
+        self._cams = cams  # keep alive for the call
+        rdesc = _rays_desc(None, None, num_rays, self.num_samples, self.delta_step, self.stratified,
+                           self.seed, self.term_threshold, cameras=cams)
+        return self._launch(rdesc, None, rgba_out, zero_grad)

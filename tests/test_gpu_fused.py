@@ -1,0 +1,199 @@
+"""Fused kernels against the oracle (oracle/torch_port.py, pinned to the reference by
+tests/golden) on seeded synthetic scenes: bit-exact voxel indices, forward within 1e-5
+relative, gradients within 1e-4 of the largest entry; plus the fp64 adjoint against
+central finite differences, BF16 storage against the fp32 path, and edge sizes."""
+import numpy as np
+import pytest
+import torch
+
+import plenoxels_gb300 as pg
+import scenes
+from oracle import torch_port as tp
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def _grad_close(got, ref, rel=1e-4):
+    got = got.detach().cpu().double().numpy() if torch.is_tensor(got) else got
+    ref = ref.detach().cpu().double().numpy() if torch.is_tensor(ref) else ref
+    scale = np.abs(ref).max()
+    err = np.abs(got - ref).max()
+    assert err <= rel * scale + 1e-12, f"max grad error {err:.3e} vs scale {scale:.3e}"
+
+
+def _scene(side, n_cams, rays, seed, near=2.0, far=6.0, S=64, amp=(5, 20), neg=0.0):
+    grid = torch.from_numpy(scenes.make_grid(side, 4, seed, amp=amp, negative_frac=neg))
+    T = torch.from_numpy(scenes.make_cameras(n_cams, seed + 1))
+    imgs = torch.from_numpy(scenes.make_images(n_cams, 32, 32, seed + 2))
+    o, d, target = tp.camera_batch(T, 0.691, imgs, rays, seed + 3, near)
+    delta = (far - near) / S
+    return grid, T, imgs, o, d, target, delta
+
+
+CASES = [
+    # side, cams, rays, S, mode, stratified, amp, neg
+    (32, 3, 300, 64, "trilinear", False, (5, 20), 0.0),
+    (32, 3, 300, 64, "nearest", False, (0.2, 2), 0.05),
+    (48, 4, 200, 256, "trilinear", True, (0.2, 3), 0.02),
+    (48, 4, 200, 256, "nearest", True, (5, 20), 0.0),
+    (24, 2, 100, 600, "trilinear", False, (0.1, 1), 0.0),   # reference default S, 3 chunks
+    (24, 2, 64, 512, "trilinear", True, (0.1, 1), 0.0),     # 16 slots per lane
+    (16, 2, 50, 17, "nearest", False, (0.5, 2), 0.1),       # ragged S
+    (16, 1, 33, 1, "trilinear", False, (0.5, 2), 0.1),      # single sample
+]
+
+
+@pytest.mark.parametrize("side,cams,rays,S,mode,strat,amp,neg", CASES)
+def test_fused_matches_oracle(side, cams, rays, S, mode, strat, amp, neg):
+    grid, T, imgs, o, d, target, delta = _scene(side, cams, rays, side + S, S=S, amp=amp, neg=neg)
+    pd = scenes.points_distance(side)
+    gmin = tp.grid_min(grid.shape, pd)
+    jitter = tp.jitter_for(9, rays, S) if strat else None
+    # oracle (CPU)
+    g_ref = grid.clone().requires_grad_(True)
+    px_ref = tp.render(g_ref, o, d, S, delta, gmin, pd, mode, True, jitter)
+    idx_ref, inb_ref = tp.sample_indices(o, d, S, delta, gmin, pd, grid.shape, mode, jitter)
+    loss_ref = torch.nn.functional.mse_loss(px_ref, target)
+    loss_ref.backward()
+    # CUDA
+    g = grid.to(DEV).requires_grad_(True)
+    od, dd = o.to(DEV), d.to(DEV)
+    idx, inb = pg.render_sample_indices(g, od, dd, delta, S, pd, mode=mode, stratified=strat, seed=9)
+    np.testing.assert_array_equal(idx.cpu().numpy().reshape(-1), idx_ref.numpy().reshape(-1))
+    np.testing.assert_array_equal(inb.cpu().numpy().reshape(-1), inb_ref.numpy())
+    px = pg.render_rays(g, od, dd, delta, S, pd, mode=mode, stratified=strat, seed=9)
+    np.testing.assert_allclose(px.detach().cpu().numpy(), px_ref.detach().numpy(), rtol=1e-5, atol=2e-6)
+    loss = torch.nn.functional.mse_loss(px, target.to(DEV))
+    loss.backward()
+    _grad_close(g.grad, g_ref.grad)
+    # fused training step: same loss and gradient in one launch
+    step = pg.FusedTrainStep(g.detach(), pd, S, delta, mode=mode, stratified=strat, seed=9)
+    l2 = step.step_rays(od, dd, target.to(DEV))
+    np.testing.assert_allclose(float(l2), float(loss_ref), rtol=1e-5)
+    _grad_close(step.grad, g_ref.grad)
+
+
+@pytest.mark.parametrize("mode", ["nearest", "trilinear"])
+def test_camera_rays_generated_in_kernel(mode):
+    side, S, rays = 40, 128, 1000
+    grid = torch.from_numpy(scenes.make_grid(side, 4, 3, amp=(0.3, 3)))
+    T = torch.from_numpy(scenes.make_cameras(7, 4))
+    imgs = torch.from_numpy(scenes.make_images(7, 24, 24, 5))
+    pd, near, far = scenes.points_distance(side), 2.0, 6.0
+    delta = (far - near) / S
+    o, d, target = tp.camera_batch(T, 0.691, imgs, rays, 77, near)
+    gmin = tp.grid_min(grid.shape, pd)
+    g_ref = grid.clone().requires_grad_(True)
+    px_ref = tp.render(g_ref, o, d, S, delta, gmin, pd, mode, True, tp.jitter_for(5, rays, S))
+    loss_ref = torch.nn.functional.mse_loss(px_ref, target)
+    loss_ref.backward()
+    g = grid.to(DEV)
+    step = pg.FusedTrainStep(g, pd, S, delta, mode=mode, stratified=True, seed=5)
+    rgba = torch.empty(rays, 4, device=DEV)
+    loss = step.step_cameras(T.to(DEV), imgs.to(DEV), 0.691, rays, 77, near=near, rgba_out=rgba)
+    np.testing.assert_allclose(rgba.cpu().numpy(), px_ref.detach().numpy(), rtol=1e-5, atol=2e-6)
+    np.testing.assert_allclose(float(loss), float(loss_ref), rtol=1e-5)
+    _grad_close(step.grad, g_ref.grad)
+
+
+def test_fp64_adjoint_matches_central_differences():
+    """32^3 fp64 grid, 1024 rays, 64 samples, trilinear: the fp64 adjoint against
+    central differences (eps 1e-4) of the fp64 oracle on 200 random entries, and against
+    the oracle's autograd gradient over all cells."""
+    side, S, rays = 32, 64, 1024
+    grid = torch.from_numpy(scenes.make_grid(side, 3, 21, amp=(0.2, 0.9))).double()
+    T = torch.from_numpy(scenes.make_cameras(4, 22))
+    imgs = torch.from_numpy(scenes.make_images(4, 16, 16, 23))
+    o, d, target = tp.camera_batch(T, 0.691, imgs, rays, 24, 2.0)
+    o, d, target = o.double(), d.double(), target.double()
+    pd, delta = scenes.points_distance(side), 4.0 / S
+    gmin = tp.grid_min(grid.shape, pd, torch.float64)
+    g = grid.to(DEV).requires_grad_(True)
+    px = pg.render_rays(g, o.to(DEV), d.to(DEV), delta, S, pd, grid_min=gmin.tolist())
+    loss = torch.nn.functional.mse_loss(px, target.to(DEV))
+    loss.backward()
+    grad = g.grad.cpu().numpy()
+    g_ref = grid.clone().requires_grad_(True)
+    tp.train_loss(g_ref, o, d, target, S, delta, gmin, pd).backward()
+    _grad_close(grad, g_ref.grad, rel=1e-10)
+    # central differences on entries with a non-zero gradient (inside the clip range)
+    rng = np.random.default_rng(0)
+    cand = np.argwhere(np.abs(grad) > 1e-8 * np.abs(grad).max())
+    pick = cand[rng.choice(len(cand), size=min(200, len(cand)), replace=False)]
+    eps = 1e-4
+    worst = 0.0
+    with torch.no_grad():
+        for i, j, k, c in pick:
+            gp = grid.clone(); gp[i, j, k, c] += eps
+            gm = grid.clone(); gm[i, j, k, c] -= eps
+            lp = tp.train_loss(gp, o, d, target, S, delta, gmin, pd)
+            lm = tp.train_loss(gm, o, d, target, S, delta, gmin, pd)
+            fd = float(lp - lm) / (2 * eps)
+            worst = max(worst, abs(fd - grad[i, j, k, c]) / max(abs(fd), 1e-3 * np.abs(grad).max()))
+    assert worst < 1e-4, f"max relative error vs central differences {worst:.2e}"
+
+
+def test_bf16_storage_matches_fp32_on_rounded_grid():
+    side, S, rays = 48, 256, 500
+    grid = torch.from_numpy(scenes.make_grid(side, 6, 31, amp=(0.3, 3)))
+    g16 = grid.to(torch.bfloat16)
+    g32 = g16.float()  # the values the bf16 kernel sees
+    T = torch.from_numpy(scenes.make_cameras(3, 32))
+    imgs = torch.from_numpy(scenes.make_images(3, 16, 16, 33))
+    o, d, target = tp.camera_batch(T, 0.691, imgs, rays, 34, 2.0)
+    pd, delta = scenes.points_distance(side), 4.0 / S
+    a = pg.FusedTrainStep(g16.to(DEV), pd, S, delta)
+    b = pg.FusedTrainStep(g32.to(DEV), pd, S, delta)
+    ra, rb = torch.empty(rays, 4, device=DEV), torch.empty(rays, 4, device=DEV)
+    la = a.step_rays(o.to(DEV), d.to(DEV), target.to(DEV), rgba_out=ra)
+    lb = b.step_rays(o.to(DEV), d.to(DEV), target.to(DEV), rgba_out=rb)
+    assert a.grad.dtype == torch.float32
+    np.testing.assert_allclose(ra.cpu().numpy(), rb.cpu().numpy(), rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(float(la), float(lb), rtol=1e-6)
+    _grad_close(a.grad, b.grad, rel=1e-6)
+
+
+def test_empty_batches_and_zero_samples():
+    grid = torch.rand(8, 8, 8, 4, device=DEV, requires_grad=True)
+    o = torch.zeros(0, 3, device=DEV)
+    px = pg.render_rays(grid, o, o, 0.1, 16, 0.25)
+    assert px.shape == (0, 4)
+    o1 = torch.tensor([[0.0, 0.0, -3.0]], device=DEV)
+    d1 = torch.tensor([[0.0, 0.0, 1.0]], device=DEV)
+    px = pg.render_rays(grid, o1, d1, 0.1, 0, 0.25)
+    assert px.shape == (1, 4) and float(px.abs().sum()) == 0.0
+    px.sum().backward()
+    assert float(grid.grad.abs().sum()) == 0.0
+
+
+def test_non_contiguous_grid_view_gets_gradient():
+    """A permuted view (the pooled grid of scripts/train.py:118) is made contiguous by the
+    wrapper and autograd carries the gradient back through the permute."""
+    base = torch.rand(4, 16, 16, 16, device=DEV, requires_grad=True)
+    view = base.permute(1, 2, 3, 0)
+    assert not view.is_contiguous()
+    o = torch.tensor([[0.05, -0.02, -3.0]], device=DEV)
+    d = torch.tensor([[0.0, 0.0, 1.0]], device=DEV)
+    px = pg.render_rays(view, o, d, 0.05, 120, 3.0 / 16)
+    px.sum().backward()
+    ref_grid = view.detach().cpu().requires_grad_(True)
+    ref = tp.render(ref_grid, o.cpu(), d.cpu(), 120, 0.05, tp.grid_min(ref_grid.shape, 3.0 / 16),
+                    3.0 / 16)
+    ref.sum().backward()
+    np.testing.assert_allclose(px.detach().cpu().numpy(), ref.detach().numpy(), rtol=1e-5, atol=1e-6)
+    _grad_close(base.grad.permute(1, 2, 3, 0), ref_grid.grad)
+
+
+def test_determinism_of_forward_and_loss():
+    grid, T, imgs, o, d, target, delta = _scene(32, 3, 500, 5, S=128)
+    pd = scenes.points_distance(32)
+    g = grid.to(DEV)
+    step = pg.FusedTrainStep(g, pd, 128, delta)
+    r1, r2 = torch.empty(500, 4, device=DEV), torch.empty(500, 4, device=DEV)
+    l1 = float(step.step_rays(o.to(DEV), d.to(DEV), target.to(DEV), rgba_out=r1))
+    g1 = step.grad.clone()
+    l2 = float(step.step_rays(o.to(DEV), d.to(DEV), target.to(DEV), rgba_out=r2))
+    assert l1 == l2
+    assert torch.equal(r1, r2)
+    _grad_close(step.grad, g1, rel=1e-6)  # atomics: order may differ, values agree
