@@ -159,8 +159,8 @@ int pgb_render_fwd(const pgb_grid* grid, const pgb_rays* rays, void* rgba_out, p
   int st = check_grid(grid);
   if (st) return st;
   if ((st = check_rays(grid, rays, false))) return st;
-  if (!rgba_out) return PGB_ERR_ARG;
   if (rays->num_rays == 0) return PGB_OK;
+  if (!rgba_out) return PGB_ERR_ARG;
   if (grid->dtype == PGB_F64)
     return render_common<double>(grid, rays, kForward, rgba_out, nullptr, nullptr, 1.0, nullptr,
                                  nullptr, nullptr, stream);
@@ -173,9 +173,9 @@ int pgb_render_bwd(const pgb_grid* grid, const pgb_rays* rays, const void* d_rgb
   int st = check_grid(grid);
   if (st) return st;
   if ((st = check_rays(grid, rays, false))) return st;
+  if (rays->num_rays == 0) return PGB_OK;
   if (!d_rgba || !grad_cells) return PGB_ERR_ARG;
   if (!aligned(grad_cells, 16)) return PGB_ERR_ALIGN;
-  if (rays->num_rays == 0) return PGB_OK;
   if (grid->dtype == PGB_F64)
     return render_common<double>(grid, rays, kBackward, nullptr, d_rgba, nullptr, 1.0, grad_cells,
                                  nullptr, nullptr, stream);
@@ -208,8 +208,8 @@ int pgb_render_sample_indices(const pgb_grid* grid, const pgb_rays* rays, int64_
   int st = check_grid(grid);
   if (st) return st;
   if ((st = check_rays(grid, rays, false))) return st;
-  if (!index_out && !inbounds_out) return PGB_ERR_ARG;
   if (rays->num_rays == 0 || rays->num_samples == 0) return PGB_OK;
+  if (!index_out && !inbounds_out) return PGB_ERR_ARG;
   if (grid->dtype == PGB_F64) {
     RenderArgs<double> a = render_args<double>(grid, rays);
     return op_render_indices_f64(a, grid->mode, index_out, inbounds_out, stream);
@@ -222,8 +222,9 @@ int pgb_generate_rays(const float* transforms, int32_t num_cameras, int64_t rays
                       float camera_angle_x, const float* images, int32_t height, int32_t width,
                       const float* uv, int32_t even_spread, float* dirs_out, float* pixels_out,
                       int32_t* status_out, pgb_stream_t stream) {
-  if (!transforms || !images || !dirs_out || !pixels_out) return PGB_ERR_ARG;
   if (num_cameras < 0 || rays_per_camera < 0 || height <= 0 || width <= 0) return PGB_ERR_ARG;
+  if ((int64_t)num_cameras * rays_per_camera == 0) return PGB_OK;
+  if (!transforms || !images || !dirs_out || !pixels_out) return PGB_ERR_ARG;
   if (!aligned(images, 16) || !aligned(pixels_out, 16)) return PGB_ERR_ALIGN;
   int side = 0;
   if (even_spread) {
@@ -241,9 +242,9 @@ int pgb_generate_rays(const float* transforms, int32_t num_cameras, int64_t rays
 int pgb_sample_points(const float* transforms, int32_t num_cameras, int64_t rays_per_camera,
                       const float* dirs, int32_t num_samples, float delta_step, float* samples_out,
                       pgb_stream_t stream) {
-  if (!transforms || !dirs || !samples_out) return PGB_ERR_ARG;
   if (num_cameras < 0 || rays_per_camera < 0 || num_samples < 0) return PGB_ERR_ARG;
   if ((int64_t)num_cameras * rays_per_camera * num_samples == 0) return PGB_OK;
+  if (!transforms || !dirs || !samples_out) return PGB_ERR_ARG;
   return op_sample_points(transforms, num_cameras, rays_per_camera, dirs, num_samples, delta_step,
                           samples_out, stream);
 }
@@ -255,8 +256,9 @@ int pgb_coords_min(const float* coords, int64_t count, float* min_out, pgb_strea
 
 int pgb_normalize_samples(const float* samples, int64_t count, const float* grid_min,
                           float points_distance, float* out, pgb_stream_t stream) {
-  if (!samples || !grid_min || !out || count < 0) return PGB_ERR_ARG;
+  if (count < 0) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!samples || !grid_min || !out) return PGB_ERR_ARG;
   return op_normalize(samples, count, grid_min, points_distance, out, stream);
 }
 
@@ -264,8 +266,9 @@ int pgb_nearest_gather(const pgb_grid* grid, const void* normalized, int64_t cou
                        uint8_t* inbounds_out, int64_t* index_out, pgb_stream_t stream) {
   int st = check_grid(grid);
   if (st) return st;
-  if (!normalized || !vals_out || count < 0) return PGB_ERR_ARG;
+  if (count < 0) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!normalized || !vals_out) return PGB_ERR_ARG;
   if (grid->dtype == PGB_F64)
     return op_nearest_gather_f64(grid_params<double>(grid), normalized, count, vals_out,
                                  inbounds_out, index_out, stream);
@@ -277,9 +280,10 @@ int pgb_nearest_scatter(const pgb_grid* grid, const void* normalized, int64_t co
                         const void* d_vals, void* grad_cells, pgb_stream_t stream) {
   int st = check_grid(grid);
   if (st) return st;
-  if (!normalized || !d_vals || !grad_cells || count < 0) return PGB_ERR_ARG;
-  if (!aligned(grad_cells, 16)) return PGB_ERR_ALIGN;
+  if (count < 0) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!normalized || !d_vals || !grad_cells) return PGB_ERR_ARG;
+  if (!aligned(grad_cells, 16)) return PGB_ERR_ALIGN;
   if (grid->dtype == PGB_F64)
     return op_nearest_scatter_f64(grid_params<double>(grid), normalized, count, d_vals, grad_cells,
                                   stream);
@@ -299,8 +303,9 @@ int pgb_gather_cells(const pgb_grid* grid, const int64_t* indices, int64_t count
                      int32_t* status_out, pgb_stream_t stream) {
   int st = check_grid(grid);
   if (st) return st;
-  if (!indices || !vals_out || count < 0) return PGB_ERR_ARG;
+  if (count < 0) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!indices || !vals_out) return PGB_ERR_ARG;
   if (grid->dtype == PGB_F64)
     return op_gather_cells_f64(grid_params<double>(grid), indices, count, vals_out, status_out, stream);
   return op_gather_cells_f32(grid_params<float>(grid), grid->dtype == PGB_BF16, indices, count,
@@ -312,9 +317,10 @@ int pgb_scatter_cells(const pgb_grid* grid, const int64_t* indices, int64_t coun
                       pgb_stream_t stream) {
   int st = check_grid(grid);
   if (st) return st;
-  if (!indices || !d_vals || !grad_cells || count < 0) return PGB_ERR_ARG;
-  if (!aligned(grad_cells, 16)) return PGB_ERR_ALIGN;
+  if (count < 0) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!indices || !d_vals || !grad_cells) return PGB_ERR_ARG;
+  if (!aligned(grad_cells, 16)) return PGB_ERR_ALIGN;
   if (grid->dtype == PGB_F64)
     return op_scatter_cells_f64(grid_params<double>(grid), indices, count, d_vals, grad_cells,
                                 status_out, stream);
@@ -324,26 +330,28 @@ int pgb_scatter_cells(const pgb_grid* grid, const int64_t* indices, int64_t coun
 
 int pgb_corner_indices(const void* normalized, int32_t dtype, int64_t count, int64_t* corners_out,
                        pgb_stream_t stream) {
-  if (!normalized || !corners_out || count < 0) return PGB_ERR_ARG;
-  if (dtype != PGB_F32 && dtype != PGB_F64) return PGB_ERR_ARG;
+  if (count < 0 || (dtype != PGB_F32 && dtype != PGB_F64)) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!normalized || !corners_out) return PGB_ERR_ARG;
   return op_corner_indices(normalized, dtype == PGB_F64, count, corners_out, stream);
 }
 
 int pgb_in_bounds(const void* indices, int32_t index_kind, int64_t count, const int32_t dims[3],
                   uint8_t* out, pgb_stream_t stream) {
-  if (!indices || !dims || !out || count < 0) return PGB_ERR_ARG;
+  if (count < 0 || !dims) return PGB_ERR_ARG;
   if (index_kind != PGB_INDEX_F32 && index_kind != PGB_INDEX_F64 && index_kind != PGB_INDEX_I64)
     return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!indices || !out) return PGB_ERR_ARG;
   const int d[3] = {dims[0], dims[1], dims[2]};
   return op_in_bounds(indices, index_kind, count, d, out, stream);
 }
 
 int pgb_wrap_indices(int64_t* indices, int64_t count, const int32_t dims[3], pgb_stream_t stream) {
-  if (!indices || !dims || count < 0) return PGB_ERR_ARG;
+  if (!dims || count < 0) return PGB_ERR_ARG;
   if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!indices) return PGB_ERR_ARG;
   const int d[3] = {dims[0], dims[1], dims[2]};
   return op_wrap(indices, count, d, stream);
 }
@@ -352,8 +360,9 @@ int pgb_trilinear_gather(const pgb_grid* grid, const void* normalized, const int
                          int64_t count, void* out, int32_t* status_out, pgb_stream_t stream) {
   int st = check_grid(grid);
   if (st) return st;
-  if (!normalized || !corners || !out || count < 0) return PGB_ERR_ARG;
+  if (count < 0) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!normalized || !corners || !out) return PGB_ERR_ARG;
   if (grid->dtype == PGB_F64)
     return op_trilinear_gather_f64(grid_params<double>(grid), normalized, corners, count, out,
                                    status_out, stream);
@@ -366,9 +375,10 @@ int pgb_trilinear_scatter(const pgb_grid* grid, const void* normalized, const in
                           pgb_stream_t stream) {
   int st = check_grid(grid);
   if (st) return st;
-  if (!normalized || !corners || !d_out || !grad_cells || count < 0) return PGB_ERR_ARG;
-  if (!aligned(grad_cells, 16)) return PGB_ERR_ALIGN;
+  if (count < 0) return PGB_ERR_ARG;
   if (count == 0) return PGB_OK;
+  if (!normalized || !corners || !d_out || !grad_cells) return PGB_ERR_ARG;
+  if (!aligned(grad_cells, 16)) return PGB_ERR_ALIGN;
   if (grid->dtype == PGB_F64)
     return op_trilinear_scatter_f64(grid_params<double>(grid), normalized, corners, count, d_out,
                                     grad_cells, status_out, stream);
@@ -378,28 +388,31 @@ int pgb_trilinear_scatter(const pgb_grid* grid, const void* normalized, const in
 
 int pgb_composite_fwd(const void* samples, int32_t dtype, int64_t num_rays, int32_t num_samples,
                       void* out, pgb_stream_t stream) {
-  if (!samples || !out || num_rays < 0 || num_samples < 0) return PGB_ERR_ARG;
+  if (num_rays < 0 || num_samples < 0) return PGB_ERR_ARG;
   if (dtype != PGB_F32 && dtype != PGB_F64) return PGB_ERR_ARG;
   if (num_samples > composite_max_samples()) return PGB_ERR_UNSUPPORTED;
-  if (!aligned(samples, 16)) return PGB_ERR_ALIGN;
   if (num_rays == 0) return PGB_OK;
+  if (!out || (num_samples > 0 && !samples)) return PGB_ERR_ARG;
+  if (!aligned(samples, 16)) return PGB_ERR_ALIGN;
   return op_composite(samples, dtype == PGB_F64, num_rays, num_samples, nullptr, out, 0, stream);
 }
 
 int pgb_composite_bwd(const void* samples, int32_t dtype, int64_t num_rays, int32_t num_samples,
                       const void* d_out, void* d_samples, pgb_stream_t stream) {
-  if (!samples || !d_out || !d_samples || num_rays < 0 || num_samples < 0) return PGB_ERR_ARG;
+  if (num_rays < 0 || num_samples < 0) return PGB_ERR_ARG;
   if (dtype != PGB_F32 && dtype != PGB_F64) return PGB_ERR_ARG;
   if (num_samples > composite_max_samples()) return PGB_ERR_UNSUPPORTED;
+  if (num_rays == 0 || num_samples == 0) return PGB_OK;
+  if (!samples || !d_out || !d_samples) return PGB_ERR_ARG;
   if (!aligned(samples, 16)) return PGB_ERR_ALIGN;
-  if (num_rays == 0) return PGB_OK;
   return op_composite(samples, dtype == PGB_F64, num_rays, num_samples, d_out, d_samples, 1, stream);
 }
 
 int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream) {
-  if (!ptr || bytes < 0) return PGB_ERR_ARG;
-  if (!aligned(ptr, 16)) return PGB_ERR_ALIGN;
+  if (bytes < 0) return PGB_ERR_ARG;
   if (bytes == 0) return PGB_OK;
+  if (!ptr) return PGB_ERR_ARG;
+  if (!aligned(ptr, 16)) return PGB_ERR_ALIGN;
   return op_fill_zero(ptr, bytes, stream);
 }
 

@@ -78,10 +78,15 @@ struct Ray {
   uint64_t h;  // stratification stream of this ray
 };
 
-// Euclidean norm as the reference's CPU torch.norm evaluates a 3-vector:
-// sqrt(fma(z, z, fma(y, y, x * x))).
+// Euclidean norm of a 3-vector as the reference's CPU torch.norm evaluates it. Over a
+// contiguous last dimension (the direction tensor) it accumulates with FMAs:
+// sqrt(fma(z, z, fma(y, y, x * x))); over a strided view (the camera axes T[:, :3, i])
+// it rounds every product and sum: sqrt((x*x + y*y) + z*z).
 __device__ __forceinline__ float norm3_ref(float x, float y, float z) {
   return rsqrt_exact(rfma(z, z, rfma(y, y, rmul(x, x))));
+}
+__device__ __forceinline__ float norm3_strided_ref(float x, float y, float z) {
+  return rsqrt_exact(radd(radd(rmul(x, x), rmul(y, y)), rmul(z, z)));
 }
 
 // Direction of a camera ray from uniforms (u, v), src/ray_sampling.py:215-262, rounded
@@ -92,7 +97,7 @@ __device__ __forceinline__ void camera_direction(const float* T, float fov, floa
   const float xa0 = T[0], xa1 = T[4], xa2 = T[8];
   const float ya0 = T[1], ya1 = T[5], ya2 = T[9];
   const float za0 = -T[2], za1 = -T[6], za2 = -T[10];
-  const float aspect = rdiv(norm3_ref(xa0, xa1, xa2), norm3_ref(ya0, ya1, ya2));
+  const float aspect = rdiv(norm3_strided_ref(xa0, xa1, xa2), norm3_strided_ref(ya0, ya1, ya2));
   const float ru = rmul(fov, rsub(u, 0.5f));
   const float rv = -rmul(rmul(fov, rdiv(1.0f, aspect)), rsub(v, 0.5f));
   const float e0 = radd(radd(rmul(ru, xa0), rmul(rv, ya0)), za0);
