@@ -141,7 +141,7 @@ int render_common(const pgb_grid* g, const pgb_rays* r, int phase, void* rgba_ou
   a.loss_out = (Real*)loss_out;
   if (workspace) {
     a.partials = (double*)workspace;
-    a.counter = (unsigned*)((char*)workspace + sizeof(double) * kMaxTrainBlocks);
+    a.counter = (unsigned*)((char*)workspace + sizeof(double) * kMaxTrainWarps);
   }
   a.loss_w = loss_w;
   a.inv_count = r->num_rays > 0 ? 1.0 / (4.0 * (double)r->num_rays) : std::nan("");
@@ -184,7 +184,7 @@ int pgb_render_bwd(const pgb_grid* grid, const pgb_rays* rays, const void* d_rgb
 }
 
 int64_t pgb_train_workspace_bytes(void) {
-  return (int64_t)sizeof(double) * kMaxTrainBlocks + 256;
+  return (int64_t)sizeof(double) * kMaxTrainWarps + 256;
 }
 
 int pgb_render_train(const pgb_grid* grid, const pgb_rays* rays, const void* target,

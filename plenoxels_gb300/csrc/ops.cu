@@ -412,6 +412,21 @@ __device__ __forceinline__ void load_sample<float>(const float* p, float v[4]) {
 
 constexpr int kCompK = 8;
 
+// Exclusive transmittance of every sample of a register chunk from the chunk's starting
+// T; returns T after the chunk.
+template <typename Real, int K>
+__device__ __forceinline__ Real scan_chunk(const Real v[K][4], Real T, int lane, Real Ts[K]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const Real incl = warp_incl_prod(Real(1) - v[k][3], lane);
+    Real excl = __shfl_up_sync(kFull, incl, 1);
+    if (lane == 0) excl = Real(1);
+    Ts[k] = T * excl;
+    T *= __shfl_sync(kFull, incl, kWarp - 1);
+  }
+  return T;
+}
+
 template <typename Real>
 __device__ __forceinline__ void load_comp_chunk(const Real* base, int S, int c, int lane,
                                                 Real v[kCompK][4]) {

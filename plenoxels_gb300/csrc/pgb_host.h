@@ -14,8 +14,8 @@ template <typename Real> struct RenderArgs;
 // Counts one kernel launch and converts the launch status into a PGB status.
 int after_launch();
 
-// Largest grid the fused training kernel may use (size of its block-partial table).
-constexpr int kMaxTrainBlocks = 8192;
+// Most warps the fused training kernel may use (size of its per-warp loss table).
+constexpr int kMaxTrainWarps = 32768;
 // Samples per chunk are 32 * K; a ray may span at most this many chunks.
 constexpr int kMaxChunks = 32;
 // Largest samples-per-ray the fused kernels accept.

@@ -279,43 +279,87 @@ __device__ __forceinline__ void sample_scatter(const GridP<Real>& g, Real* grad,
     trilinear_corners(g, nx, ny, nz, q);
     const Real wx = q.w[0], wy = q.w[1], wz = q.w[2];
     const Real ux = rsub(Real(1), wx), uy = rsub(Real(1), wy), uz = rsub(Real(1), wz);
+    // corner weights, corner order of src/grid_functions.py:16-24
+    const Real wyz[4] = {wy * wz, wy * uz, uy * wz, uy * uz};
+    const uint64_t rowc = (uint64_t)q.c[0] * (uint64_t)g.Y, rowf = (uint64_t)q.f[0] * (uint64_t)g.Y;
 #pragma unroll
     for (int corner = 0; corner < 8; ++corner) {
-      const Real sz = (corner & 1) ? uz : wz;
-      const Real sy = (corner & 2) ? uy : wy;
-      const Real sx = (corner & 4) ? ux : wx;
+      const Real wc = ((corner & 4) ? ux : wx) * wyz[corner & 3];
+      const uint32_t cb = bits >> (4 * corner);
+      if ((cb & 0xfu) == 0u) continue;
       Real gv[4];
       bool any = false;
 #pragma unroll
       for (int ch = 0; ch < 4; ++ch) {
-        const Real t = rmul(rmul(rmul(dv[ch], sz), sy), sx);
-        gv[ch] = ((bits >> (4 * corner + ch)) & 1u) ? t : Real(0);
+        gv[ch] = ((cb >> ch) & 1u) ? dv[ch] * wc : Real(0);
         any |= gv[ch] != Real(0);
       }
       if (any) {
-        const int ix = (corner & 4) ? q.f[0] : q.c[0];
+        const uint64_t row = (corner & 4) ? rowf : rowc;
         const int iy = (corner & 2) ? q.f[1] : q.c[1];
         const int iz = (corner & 1) ? q.f[2] : q.c[2];
-        grad_add(grad, cell_index(g, ix, iy, iz), gv);
+        grad_add(grad, (row + (uint64_t)iy) * (uint64_t)g.Z + (uint64_t)iz, gv);
       }
     }
   }
 }
 
-// Gathers chunk `c` (K slots) of a ray into registers.
-template <typename Real, typename Store, int MODE, int K>
+// Tuning knobs (compile-time; the shipped values are the measured best on GB300).
+#ifndef PGB_RENDER_THREADS
+#define PGB_RENDER_THREADS 256
+#endif
+#ifndef PGB_RENDER_MIN_BLOCKS
+#define PGB_RENDER_MIN_BLOCKS 0
+#endif
+#ifndef PGB_GATHER_UNROLL
+#define PGB_GATHER_UNROLL 0  // 0: fully unrolled slot loop
+#endif
+#ifndef PGB_COORDS_IN_SMEM
+#define PGB_COORDS_IN_SMEM 1
+#endif
+
+constexpr int kRenderThreads = PGB_RENDER_THREADS;
+
+// Normalised coordinates of a warp's chunk kept for the reverse pass, so the adjoint does
+// not recompute the stratification hash and the three exact divisions: [3][K][32].
+template <typename Real, int K>
+struct CoordStage {
+  static constexpr int kBytesPerWarp = PGB_COORDS_IN_SMEM ? 3 * K * kWarp * (int)sizeof(Real) : 0;
+  Real* n;
+  __device__ __forceinline__ CoordStage(unsigned char* base, int warp)
+      : n(reinterpret_cast<Real*>(base + (size_t)warp * kBytesPerWarp)) {}
+  __device__ __forceinline__ void put(int k, int lane, Real x, Real y, Real z) {
+    n[(0 * K + k) * kWarp + lane] = x;
+    n[(1 * K + k) * kWarp + lane] = y;
+    n[(2 * K + k) * kWarp + lane] = z;
+  }
+  __device__ __forceinline__ void get(int k, int lane, Real& x, Real& y, Real& z) const {
+    x = n[(0 * K + k) * kWarp + lane];
+    y = n[(1 * K + k) * kWarp + lane];
+    z = n[(2 * K + k) * kWarp + lane];
+  }
+};
+
+// Gathers chunk `c` (K slots) of a ray into registers (and its coordinates into the
+// stage when the adjoint follows).
+template <typename Real, typename Store, int MODE, int K, bool ADJ>
 __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ray<Real>& ray, int c,
-                                             int lane, Real v[K][4], uint32_t bits[K]) {
+                                             int lane, Real v[K][4], uint32_t bits[K],
+                                             CoordStage<Real, K>& cs) {
+#if PGB_GATHER_UNROLL == 0
 #pragma unroll
+#else
+#pragma unroll PGB_GATHER_UNROLL
+#endif
   for (int k = 0; k < K; ++k) {
     const int s = (c * K + k) * kWarp + lane;
+    v[k][0] = v[k][1] = v[k][2] = v[k][3] = Real(0);
+    bits[k] = 0u;
     if (s < a.S) {
       Real nx, ny, nz;
       sample_coords(a, ray, s, nx, ny, nz);
       sample_value<Real, Store, MODE>(a.g, nx, ny, nz, v[k], bits[k]);
-    } else {
-      v[k][0] = v[k][1] = v[k][2] = v[k][3] = Real(0);
-      bits[k] = 0u;
+      if (ADJ && PGB_COORDS_IN_SMEM) cs.put(k, lane, nx, ny, nz);
     }
   }
 }
@@ -341,14 +385,29 @@ __device__ __forceinline__ Real pick4(const Real v[4], int i) {
   return i == 0 ? v[0] : (i == 1 ? v[1] : (i == 2 ? v[2] : v[3]));
 }
 
+template <typename Real, int K>
+constexpr int render_smem_bytes(int warps_per_block) {
+  return CoordStage<Real, K>::kBytesPerWarp * warps_per_block;
+}
+
 template <typename Real, typename Store, int MODE, int K, int PHASE>
-__global__ void __launch_bounds__(256) render_kernel(const RenderArgs<Real> a) {
+__global__ void __launch_bounds__(kRenderThreads, PGB_RENDER_MIN_BLOCKS)
+render_kernel(const RenderArgs<Real> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool ADJ = PHASE != kForward;
   const int lane = threadIdx.x & (kWarp - 1);
   const int warps_per_block = blockDim.x >> 5;
   const int64_t gw = (int64_t)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int64_t nw = (int64_t)gridDim.x * warps_per_block;
   const int nchunks = (a.S + kWarp * K - 1) / (kWarp * K);
+  CoordStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
   double loss_lane = 0.0;
+  __shared__ double s_part[32];  // per-warp loss partials (training phase)
+  __shared__ unsigned s_done;    // warps of this block that finished (training phase)
+  if (PHASE == kTrain) {
+    if (threadIdx.x == 0) s_done = 0u;
+    __syncthreads();
+  }
 
   for (int64_t r = gw; r < a.R; r += nw) {
     Ray<Real> ray;
@@ -360,10 +419,11 @@ __global__ void __launch_bounds__(256) render_kernel(const RenderArgs<Real> a) {
     Real acc[4] = {Real(0), Real(0), Real(0), Real(0)};
     Real T = Real(1);
     Real Tstart = Real(1);  // lane c: transmittance at the start of chunk c
-    int last = 0;
+    int last = -1;          // last composited chunk (-1: none, e.g. zero samples)
     for (int c = 0; c < nchunks; ++c) {
       if (lane == c) Tstart = T;
-      gather_chunk<Real, Store, MODE, K>(a, ray, c, lane, v, bits);
+      __syncwarp();
+      gather_chunk<Real, Store, MODE, K, ADJ>(a, ray, c, lane, v, bits, cs);
       T = scan_chunk<Real, K>(v, T, lane, Ts);
 #pragma unroll
       for (int k = 0; k < K; ++k) {
@@ -402,24 +462,25 @@ __global__ void __launch_bounds__(256) render_kernel(const RenderArgs<Real> a) {
     }
 
     // reverse pass over the chunks that were composited
-    Real Snext_carry = Real(0);  // S at the first sample after the current chunk
+    Real Snext_carry = Real(0);  // S at the first sample after the current slot
     for (int c = last; c >= 0; --c) {
       if (c != last) {
-        gather_chunk<Real, Store, MODE, K>(a, ray, c, lane, v, bits);
+        __syncwarp();
+        gather_chunk<Real, Store, MODE, K, true>(a, ray, c, lane, v, bits, cs);
         scan_chunk<Real, K>(v, __shfl_sync(kFull, Tstart, c), lane, Ts);
       }
+      __syncwarp();
 #pragma unroll
       for (int k = K - 1; k >= 0; --k) {
         const Real al = v[k][3];
         const Real G = gpx[0] * v[k][0] + gpx[1] * v[k][1] + gpx[2] * v[k][2] + gpx[3];
         Real fa = G * al, fb = Real(1) - al;
         warp_suffix_affine(fa, fb, lane);
-        const Real S_here = fa + fb * Snext_carry;      // S_s for this lane's sample
+        const Real S_here = fa + fb * Snext_carry;          // S_s for this lane's sample
         Real S_after = __shfl_down_sync(kFull, S_here, 1);  // S_{s+1}
         if (lane == kWarp - 1) S_after = Snext_carry;
         Snext_carry = __shfl_sync(kFull, S_here, 0);
-        const int s = (c * K + k) * kWarp + lane;
-        if (bits[k] != 0u && s < a.S) {
+        if (bits[k] != 0u) {
           const Real w = al * Ts[k];
           Real dv[4];
           dv[0] = gpx[0] * w;
@@ -427,7 +488,11 @@ __global__ void __launch_bounds__(256) render_kernel(const RenderArgs<Real> a) {
           dv[2] = gpx[2] * w;
           dv[3] = Ts[k] * (G - S_after);
           Real nx, ny, nz;
-          sample_coords(a, ray, s, nx, ny, nz);
+          if (PGB_COORDS_IN_SMEM) {
+            cs.get(k, lane, nx, ny, nz);
+          } else {
+            sample_coords(a, ray, (c * K + k) * kWarp + lane, nx, ny, nz);
+          }
           sample_scatter<Real, MODE>(a.g, a.grad, nx, ny, nz, dv, bits[k]);
         }
       }
@@ -435,30 +500,37 @@ __global__ void __launch_bounds__(256) render_kernel(const RenderArgs<Real> a) {
   }
 
   if (PHASE == kTrain) {
-    // deterministic loss: fixed-order block sum, then the last block sums the blocks
-    __shared__ double red[32];
-    __shared__ bool is_last;
+    // deterministic loss without a barrier: warps count themselves out in shared memory,
+    // the block's last warp sums the block in warp order and takes one global ticket, and
+    // the last block sums the blocks in block order
     const int wib = threadIdx.x >> 5;
-    if (lane == 0) red[wib] = loss_lane;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-      for (int i = 0; i < warps_per_block; ++i) s += red[i];
-      a.partials[blockIdx.x] = s;
-      __threadfence();
-      const unsigned done = atomicAdd(a.counter, 1u);
-      is_last = (done == gridDim.x - 1);
+    unsigned last_warp = 0;
+    if (lane == 0) {
+      s_part[wib] = loss_lane;
+      __threadfence_block();
+      last_warp = atomicAdd(&s_done, 1u) == (unsigned)warps_per_block - 1u;
     }
-    __syncthreads();
-    if (is_last && wib == 0) {
-      __threadfence();
-      double s = 0.0;
-      for (unsigned i = lane; i < gridDim.x; i += kWarp)
-        s += *((volatile double*)a.partials + i);
-      s = warp_sum(s);
+    last_warp = __shfl_sync(kFull, last_warp, 0);
+    if (last_warp) {
+      unsigned last_block = 0;
       if (lane == 0) {
-        a.loss_out[0] = (Real)(a.loss_w * s * a.inv_count);
-        *a.counter = 0u;
+        __threadfence_block();
+        double sum = 0.0;
+        for (int i = 0; i < warps_per_block; ++i) sum += ((volatile double*)s_part)[i];
+        a.partials[blockIdx.x] = sum;
+        __threadfence();
+        last_block = atomicAdd(a.counter, 1u) == gridDim.x - 1u;
+      }
+      last_block = __shfl_sync(kFull, last_block, 0);
+      if (last_block) {
+        __threadfence();
+        double sum = 0.0;
+        for (unsigned i = lane; i < gridDim.x; i += kWarp) sum += *((volatile double*)a.partials + i);
+        sum = warp_sum(sum);
+        if (lane == 0) {
+          a.loss_out[0] = (Real)(a.loss_w * sum * a.inv_count);
+          *a.counter = 0u;
+        }
       }
     }
   }

@@ -12,12 +12,25 @@ namespace pgb {
 
 template <typename Real, typename Store, int MODE, int K, int PHASE>
 int launch_render_k(const RenderArgs<Real>& a, cudaStream_t s) {
-  constexpr int kThreads = 256;
+  constexpr int kThreads = kRenderThreads;
   constexpr int kWarpsPerBlock = kThreads / kWarp;
+  constexpr int kSmem = render_smem_bytes<Real, K>(kWarpsPerBlock);
+  // the dynamic shared-memory opt-in (dynamic + static may pass 48 KiB) is per device:
+  // set it on first use of each device
+  static int configured[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
+    if (cudaFuncSetAttribute(render_kernel<Real, Store, MODE, K, PHASE>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem) != cudaSuccess)
+      return PGB_ERR_LAUNCH;
+    configured[dev] = 1;
+  }
   int64_t blocks = (a.R + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  blocks = std::min<int64_t>(blocks, PHASE == kTrain ? kMaxTrainBlocks : (int64_t)1 << 20);
+  blocks = std::min<int64_t>(blocks, PHASE == kTrain ? kMaxTrainWarps / kWarpsPerBlock
+                                                     : (int64_t)1 << 20);
   if (blocks < 1) blocks = 1;
-  render_kernel<Real, Store, MODE, K, PHASE><<<(unsigned)blocks, kThreads, 0, s>>>(a);
+  render_kernel<Real, Store, MODE, K, PHASE><<<(unsigned)blocks, kThreads, kSmem, s>>>(a);
   return after_launch();
 }
 
