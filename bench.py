@@ -250,13 +250,15 @@ def main():
     pd = 3.0 / W["grid"]
     delta = (W["far"] - W["near"]) / S
     grid, T, imgs = build_scene(dev, W)
-    step = pg.FusedTrainStep(grid, pd, S, delta, mode=W["mode"], stratified=True, seed=7)
+    from plenoxels_gb300.distributed import allreduce_gradient
+    # weak scaling: R rays per rank, each rank's MSE weighted by its share of R * world
+    step = pg.FusedTrainStep(grid, pd, S, delta, mode=W["mode"], stratified=True, seed=7,
+                             loss_weight=1.0 / world)
     stream = torch.cuda.current_stream(dev)
 
     def train(i):
         step.step_cameras(T, imgs, W["camera_angle_x"], R, 1000 * rank + i, near=W["near"])
-        if world > 1:
-            torch.distributed.all_reduce(step.grad)
+        allreduce_gradient(step.grad)
 
     for i in range(args.warmup):
         train(i)
@@ -279,8 +281,7 @@ def main():
             step.step_cameras(T, imgs, W["camera_angle_x"], R, 1000 * rank + args.warmup + i,
                               near=W["near"], zero_grad=False)
             k_end[i].record(stream)
-            if world > 1:
-                torch.distributed.all_reduce(step.grad)
+            allreduce_gradient(step.grad)
         t1.record(stream)
         torch.cuda.synchronize(dev)
     launches = pg.launch_count() - launches0
@@ -320,8 +321,7 @@ def main():
         ho, hd, ht = host[i % nb]
         dev_o.copy_(ho, non_blocking=True); dev_d.copy_(hd, non_blocking=True); dev_t.copy_(ht, non_blocking=True)
         loss = step.step_rays(dev_o, dev_d, dev_t)
-        if world > 1:
-            torch.distributed.all_reduce(step.grad)
+        allreduce_gradient(step.grad)
         loss_host[i].copy_(loss, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize(dev)
