@@ -101,6 +101,22 @@ int pgb_render_train(const pgb_grid* grid, const pgb_rays* rays, const void* tar
                      void* workspace, pgb_stream_t stream);
 int64_t pgb_train_workspace_bytes(void);
 
+/* No counterpart in the reference: pgb_render_train for callers that cannot allocate
+ * device memory (their device memory is owned by another allocator, or they run a loop
+ * that must not allocate). Same arguments and results as pgb_render_train minus the
+ * workspace: the loss-reduction scratch is a fixed array inside the library (about 32 KiB per
+ * device, held by every GPU that loads the library until the process exits). It calls no
+ * cudaMalloc, cudaFree or other allocating routine.
+ * - At most PGB_NOALLOC_MAX_RAYS rays per call; more returns PGB_ERR_UNSUPPORTED.
+ * - The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ *   for that device; make that first call before any stream capture.
+ * - Every call shares the array: calls that overlap on the GPU (other streams, other host
+ *   threads) race on it. Each call clears the counter it needs on its own stream. */
+enum { PGB_NOALLOC_MAX_RAYS = 32768 };
+int pgb_render_train_noalloc(const pgb_grid* grid, const pgb_rays* rays, const void* target,
+                             double loss_weight, void* rgba_out, void* grad_cells, void* loss_out,
+                             pgb_stream_t stream);
+
 /* Debug/parity view of the fused kernels' own index math: for every sample of every
  * ray, the wrapped cell indices the lookup reads (nearest: [R,S,3]; trilinear:
  * [R,S,8,3], corner order of src/grid_functions.py:16-24) and the in-bounds flag

@@ -18,6 +18,7 @@ PGB_OK, PGB_ERR_ARG, PGB_ERR_ALIGN, PGB_ERR_LAUNCH, PGB_ERR_UNSUPPORTED = 0, -1,
 PGB_F32, PGB_BF16, PGB_F64 = 0, 1, 2
 PGB_NEAREST, PGB_TRILINEAR = 0, 1
 PGB_INDEX_F32, PGB_INDEX_F64, PGB_INDEX_I64 = 0, 1, 2
+PGB_NOALLOC_MAX_RAYS = 32768
 
 
 class PgbGrid(Structure):
@@ -65,6 +66,7 @@ _SIGNATURES = {
     "pgb_render_bwd": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P, _P]),
     "pgb_render_train": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, c_double, _P, _P, _P, _P, _P]),
     "pgb_train_workspace_bytes": (c_int64, []),
+    "pgb_render_train_noalloc": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, c_double, _P, _P, _P, _P]),
     "pgb_render_sample_indices": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P, _P]),
     "pgb_generate_rays": (c_int32, [_P, c_int32, c_int64, c_float, _P, c_int32, c_int32, _P, c_int32, _P, _P, _P, _P]),
     "pgb_sample_points": (c_int32, [_P, c_int32, c_int64, _P, c_int32, c_float, _P, _P]),
