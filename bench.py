@@ -253,7 +253,7 @@ def main():
     from plenoxels_gb300.distributed import allreduce_gradient
     # weak scaling: R rays per rank, each rank's MSE weighted by its share of R * world
     step = pg.FusedTrainStep(grid, pd, S, delta, mode=W["mode"], stratified=True, seed=7,
-                             loss_weight=1.0 / world)
+                             loss_weight=1.0 / world, overlap_zero=True)
     stream = torch.cuda.current_stream(dev)
 
     def train(i):
@@ -266,27 +266,21 @@ def main():
     if world > 1:
         torch.distributed.barrier()
 
-    # timed region: K steps, per-kernel events around the fused kernel
-    k_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    k_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    # timed region: K steps (gradient zeroing + fused kernel), events around each kernel
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = pg.launch_count()
+    step.kernel_events = []
     with Clocks(dev.index) as clk:
         time.sleep(0.3)
         t0.record(stream)
         for i in range(args.steps):
-            lib = pg.load_library()
-            lib.pgb_fill_zero(step.grad.data_ptr(), step.grad.numel() * 4, stream.cuda_stream)
-            k_start[i].record(stream)
-            step.step_cameras(T, imgs, W["camera_angle_x"], R, 1000 * rank + args.warmup + i,
-                              near=W["near"], zero_grad=False)
-            k_end[i].record(stream)
-            allreduce_gradient(step.grad)
+            train(args.warmup + i)
         t1.record(stream)
         torch.cuda.synchronize(dev)
     launches = pg.launch_count() - launches0
     ms_total = t0.elapsed_time(t1)
-    kern_ms = sum(a.elapsed_time(b) for a, b in zip(k_start, k_end)) / args.steps
+    kern_ms = sum(a.elapsed_time(b) for a, b in step.kernel_events) / args.steps
+    step.kernel_events = None
     if world > 1:
         tt = torch.tensor([ms_total], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)

@@ -168,11 +168,16 @@ class FusedTrainStep:
     can step on it. Each call zeroes the gradient first (optimizer.zero_grad semantics)
     unless zero_grad=False, in which case it accumulates like autograd does. Every call
     is asynchronous; the returned loss is a device scalar.
+
+    overlap_zero=True keeps two gradient buffers and zeroes the next step's buffer on a
+    side stream while the current step's kernel runs (the 256 MiB fill of a 256^3 grid
+    no longer sits on the critical path). A step's gradient then stays valid until the
+    next step is launched; the buffer alternates, and ``grid.grad``/``self.grad`` follow.
     """
 
     def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
                  grid_min=None, clip=True, stratified=False, seed=0, term_threshold=0.0,
-                 loss_weight=1.0):
+                 loss_weight=1.0, overlap_zero=False):
         require_cuda(grid)
         if grid.dim() != 4 or grid.shape[-1] != 4 or not grid.is_contiguous():
             raise ValueError("grid must be a contiguous [X,Y,Z,4] tensor")
@@ -192,22 +197,70 @@ class FusedTrainStep:
         lib = _lib.load()
         dev = grid.device
         self.workspace = torch.zeros(lib.pgb_train_workspace_bytes(), dtype=torch.uint8, device=dev)
-        self.grad = torch.zeros(grid.shape, dtype=self.real, device=dev)
+        self._grads = [torch.zeros(grid.shape, dtype=self.real, device=dev)]
+        self._side = None
+        if overlap_zero:
+            self._grads.append(torch.zeros(grid.shape, dtype=self.real, device=dev))
+            self._side = torch.cuda.Stream(device=dev)
+            self._zeroed = [None, None]  # event: buffer b is zero and free
+        self._cur = 0
+        self.grad = self._grads[0]
         self.loss = torch.zeros((), dtype=self.real, device=dev)
-        if grid.dtype == self.real and grid.requires_grad:
-            grid.grad = self.grad
+        self._attach()
         self._cams = None
+        self.kernel_events = None  # list of (start, end) CUDA events, when timing is wanted
+
+    def _attach(self):
+        if self.grid.dtype == self.real and self.grid.requires_grad:
+            self.grid.grad = self.grad
+
+    def _fill(self, buf, stream):
+        check(_lib.load().pgb_fill_zero(ptr(buf), buf.numel() * buf.element_size(),
+                                        stream.cuda_stream), "train step")
+
+    def _gradient_for_step(self, zero_grad):
+        main = torch.cuda.current_stream(self.grid.device)
+        if not zero_grad:
+            return self.grad
+        if self._side is None:
+            self._fill(self.grad, main)
+            return self.grad
+        b = self._cur
+        buf = self._grads[b]
+        if self._zeroed[b] is None:
+            self._fill(buf, main)
+        else:
+            main.wait_event(self._zeroed[b])
+        # zero the other buffer for the next step, after everything already queued on the
+        # main stream (its last reader, e.g. the optimizer step of the previous step)
+        o = 1 - b
+        ready = torch.cuda.Event()
+        ready.record(main)
+        self._side.wait_event(ready)
+        self._fill(self._grads[o], self._side)
+        done = torch.cuda.Event()
+        done.record(self._side)
+        self._zeroed[o] = done
+        self._cur = o
+        self.grad = buf
+        self._attach()
+        return buf
 
     def _launch(self, rdesc, target, rgba_out, zero_grad):
         lib = _lib.load()
-        s = stream_of(self.grid)
-        if zero_grad:
-            check(lib.pgb_fill_zero(ptr(self.grad), self.grad.numel() * self.grad.element_size(), s),
-                  "train step")
+        grad = self._gradient_for_step(zero_grad)
+        stream = torch.cuda.current_stream(self.grid.device)
         gdesc = _lib.make_grid(self.grid, self.grid_min, self.points_distance, self.mode, self.clip)
+        ev = None
+        if self.kernel_events is not None:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record(stream)
         check(lib.pgb_render_train(gdesc, rdesc, ptr(target), self.loss_weight, ptr(rgba_out),
-                                   ptr(self.grad), ptr(self.loss), ptr(self.workspace), s),
-              "train step")
+                                   ptr(grad), ptr(self.loss), ptr(self.workspace),
+                                   stream.cuda_stream), "train step")
+        if ev is not None:
+            ev[1].record(stream)
+            self.kernel_events.append(ev)
         return self.loss
 
     def step_rays(self, origins, dirs, target, rgba_out=None, zero_grad=True):

@@ -199,3 +199,23 @@ def test_determinism_of_forward_and_loss():
     assert l1 == l2
     assert torch.equal(r1, r2)
     _grad_close(step.grad, g1, rel=1e-6)  # atomics: order may differ, values agree
+
+
+def test_overlapped_gradient_zeroing_gives_the_same_steps():
+    """overlap_zero=True zeroes the next step's gradient buffer on a side stream; every
+    step must still see a fully zeroed buffer and produce the serial result."""
+    grid = torch.from_numpy(scenes.make_grid(32, 4, 51, amp=(0.3, 3))).to(DEV)
+    T = torch.from_numpy(scenes.make_cameras(5, 52)).to(DEV)
+    imgs = torch.from_numpy(scenes.make_images(5, 16, 16, 53)).to(DEV)
+    pd, S = scenes.points_distance(32), 128
+    a = pg.FusedTrainStep(grid, pd, S, 4.0 / S, stratified=True, seed=3, overlap_zero=True)
+    b = pg.FusedTrainStep(grid, pd, S, 4.0 / S, stratified=True, seed=3)
+    seen = set()
+    for i in range(5):
+        la = a.step_cameras(T, imgs, 0.691, 900, 100 + i, near=2.0)
+        lb = b.step_cameras(T, imgs, 0.691, 900, 100 + i, near=2.0)
+        seen.add(a.grad.data_ptr())
+        torch.cuda.synchronize()
+        assert float(la) == float(lb)
+        _grad_close(a.grad, b.grad, rel=1e-6)
+    assert len(seen) == 2, "the two gradient buffers alternate"
