@@ -191,6 +191,31 @@ def torch_gpu_rate(W, grid, T, imgs, dev, steps=3):
                 sample=f"{R} rays x {S} samples, same scene, {steps} steps after 1 warm-up")
 
 
+def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup):
+    """Same workload with the grid stored as `dtype` (fp32 arithmetic and gradients):
+    rays/s of the whole step and the fused kernel's time."""
+    S, R = W["samples"], W["rays"]
+    g = grid.to(dtype)
+    step = pg.FusedTrainStep(g, 3.0 / W["grid"], S, (W["far"] - W["near"]) / S, mode=W["mode"],
+                             stratified=True, seed=7, overlap_zero=True)
+    stream = torch.cuda.current_stream(dev)
+    for i in range(warmup):
+        step.step_cameras(T, imgs, W["camera_angle_x"], R, 5000 + i, near=W["near"])
+    torch.cuda.synchronize(dev)
+    step.kernel_events = []
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for i in range(steps):
+        step.step_cameras(T, imgs, W["camera_angle_x"], R, 6000 + i, near=W["near"])
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = t0.elapsed_time(t1) / steps
+    kern = sum(a.elapsed_time(b) for a, b in step.kernel_events) / steps
+    return {"value": R / (ms / 1e3), "unit": "rays/s", "ms_per_step": ms, "kernel_ms": kern,
+            "storage": str(dtype).replace("torch.", ""), "note": "same workload, fp32 arithmetic "
+            "and gradients, cells stored in this type"}
+
+
 def run_reference_arm(args, W):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -352,6 +377,8 @@ def main():
                            parallelism=f"dp{world}" if world > 1 else "single"),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "clocks": clk.summary()}
+    line["bf16_storage"] = storage_leg(pg, grid, T, imgs, W, dev, torch.bfloat16, args.steps,
+                                       args.warmup)
     if not args.no_baselines:
         grid_cpu, T_cpu, imgs_cpu = grid.cpu(), T.cpu(), imgs.cpu()
         line["torch_gpu_baseline"] = torch_gpu_rate(W, grid, T, imgs, dev)
