@@ -62,7 +62,7 @@ int check_grid(const pgb_grid* g) {
 
 template <typename Real>
 GridP<Real> grid_params(const pgb_grid* g) {
-  GridP<Real> p;
+  GridP<Real> p = {};
   p.cells = g->cells;
   p.X = g->dims[0]; p.Y = g->dims[1]; p.Z = g->dims[2];
   p.fX = (Real)p.X; p.fY = (Real)p.Y; p.fZ = (Real)p.Z;
