@@ -124,6 +124,59 @@ int pgb_render_train_noalloc(const pgb_grid* grid, const pgb_rays* rays, const v
 int pgb_render_sample_indices(const pgb_grid* grid, const pgb_rays* rays, int64_t* index_out,
                               uint8_t* inbounds_out, pgb_stream_t stream);
 
+/* ---- batched form: many scenes, one persistent launch per training step ----
+ * Scenes of different sizes, each a dense [X,Y,Z,4] grid (BF16 or fp32 cells) whose
+ * unoccupied cells are zero and are not parameters, with a brick mask for empty-space
+ * skipping; rays of all scenes in one queue. The step is the fused training step of
+ * scripts/train.py:130-181 for every ray of every scene. No counterpart in the reference
+ * beyond that composition (the reference trains one scene, densely). */
+typedef struct {
+  const void* cells;        /* [X,Y,Z,4], dtype of the batch */
+  const uint32_t* bricks;   /* dilated brick mask (pgb_build_bricks) or NULL: no skipping */
+  const uint32_t* occupancy;/* cell bits (bit c of word c/32) or NULL: every cell is a parameter */
+  void* grad_cells;         /* [X,Y,Z,4] fp32 gradient, written only at occupied cells */
+  int32_t dims[3];          /* X, Y, Z */
+  int32_t brick_log2;       /* bricks are 2^brick_log2 cells per axis */
+  int32_t brick_dims[3];    /* ceil(dims / 2^brick_log2) */
+  float origin[3];          /* world position of cell (0,0,0) */
+  float points_distance;
+  int32_t num_samples;      /* samples per ray of this scene */
+  float delta_step;
+} pgb_scene;
+
+/* Dilated brick mask of a scene from its per-cell occupancy bits (bit c of word c/32 for
+ * cell c = (i*Y + j)*Z + k): bit b of bricks_out is set when brick b or any of its seven
+ * upper neighbours (+1 in any subset of axes) holds an occupied cell, so a sample whose
+ * floor corner lies in a clear brick reads only unoccupied cells. bricks_out must hold
+ * ceil(prod(brick_dims)/32) words and is overwritten. */
+int pgb_build_bricks(const uint32_t* cell_bits, const int32_t dims[3], int32_t brick_log2,
+                     uint32_t* bricks_out, pgb_stream_t stream);
+
+/* Packs a uint8/bool mask of count entries into bits (bit c of word c/32). */
+int pgb_pack_mask(const uint8_t* mask, int64_t count, uint32_t* bits_out, pgb_stream_t stream);
+
+/* Zeroes the gradients of all scenes of a device-resident scene table: the occupied
+ * cells where a scene has an occupancy mask (the only cells the step writes), every cell
+ * otherwise. max_cells bounds the largest scene. */
+int pgb_batch_zero_grads(const pgb_scene* scenes, int32_t num_scenes, int64_t max_cells,
+                         pgb_stream_t stream);
+
+/* One training step over all rays: ray r belongs to scene ray_scene[r] and starts at
+ * origins[r] along dirs[r]; target[r] is its pixel. scenes is a DEVICE array of
+ * num_scenes (<= 256) descriptors. Gradients accumulate into each scene's grad_cells;
+ * loss_out[0] = loss_weight * mean over all rays and channels of the squared error.
+ * term_threshold > 0 stops a ray once its transmittance falls below it (checked every
+ * 32*slots_per_lane samples). slots_per_lane in {2,4,8} and threads_per_block in
+ * {128,256} are the tile choices (0: defaults). workspace: pgb_batch_workspace_bytes(R),
+ * zeroed once before first use; the kernel leaves its counters zeroed. */
+int64_t pgb_batch_workspace_bytes(int64_t num_rays);
+int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, int32_t mode,
+                    int32_t clip, const float* origins, const float* dirs, const float* target,
+                    const int32_t* ray_scene, int64_t num_rays, float term_threshold,
+                    int32_t stratified, uint64_t seed, double loss_weight, float* rgba_out,
+                    float* loss_out, void* workspace, int32_t slots_per_lane,
+                    int32_t threads_per_block, pgb_stream_t stream);
+
 /* ---- drop-in operators, one per reference function ---- */
 
 /* src/ray_sampling.py:195-264 generate_rays_batched. uv: [C*Rc,2] uniforms in [0,1)

@@ -60,6 +60,22 @@ class PgbRays(Structure):
     ]
 
 
+class PgbScene(Structure):
+    _fields_ = [
+        ("cells", c_void_p),
+        ("bricks", c_void_p),
+        ("occupancy", c_void_p),
+        ("grad_cells", c_void_p),
+        ("dims", c_int32 * 3),
+        ("brick_log2", c_int32),
+        ("brick_dims", c_int32 * 3),
+        ("origin", c_float * 3),
+        ("points_distance", c_float),
+        ("num_samples", c_int32),
+        ("delta_step", c_float),
+    ]
+
+
 _P = c_void_p
 _SIGNATURES = {
     "pgb_render_fwd": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P]),
@@ -68,6 +84,12 @@ _SIGNATURES = {
     "pgb_train_workspace_bytes": (c_int64, []),
     "pgb_render_train_noalloc": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, c_double, _P, _P, _P, _P]),
     "pgb_render_sample_indices": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P, _P]),
+    "pgb_build_bricks": (c_int32, [_P, POINTER(c_int32), c_int32, _P, _P]),
+    "pgb_pack_mask": (c_int32, [_P, c_int64, _P, _P]),
+    "pgb_batch_zero_grads": (c_int32, [_P, c_int32, c_int64, _P]),
+    "pgb_batch_workspace_bytes": (c_int64, [c_int64]),
+    "pgb_batch_train": (c_int32, [_P, c_int32, c_int32, c_int32, c_int32, _P, _P, _P, _P, c_int64, c_float,
+                                  c_int32, c_uint64, c_double, _P, _P, _P, c_int32, c_int32, _P]),
     "pgb_generate_rays": (c_int32, [_P, c_int32, c_int64, c_float, _P, c_int32, c_int32, _P, c_int32, _P, _P, _P, _P]),
     "pgb_sample_points": (c_int32, [_P, c_int32, c_int64, _P, c_int32, c_float, _P, _P]),
     "pgb_coords_min": (c_int32, [_P, c_int64, _P, _P]),

@@ -1,0 +1,445 @@
+// Batched form of the fused training step: many scenes of different sizes, rays of
+// uneven cost (empty-space skipping, early termination), one persistent launch.
+//
+// Work distribution: a persistent grid whose warps pull rays from a global queue (one
+// atomic per ray), so rays that terminate early or cross empty space free their warp for
+// the next ray. Per ray the work is the fused training step of render.cuh (sampling,
+// lookup, compositing, MSE gradient, division-free adjoint), on the ray's own scene.
+//
+// Empty-space skipping: a sample is skipped (value 0, no gradient) when the brick of its
+// floor corner is clear in the scene's dilated brick mask, i.e. all eight trilinear
+// corners (and the nearest cell) are unoccupied. Unoccupied cells are zero and are not
+// parameters, so skipping changes neither the rendered value nor the gradient of any
+// occupied cell. Samples whose floor corner sits on an upper face (where the ceil corner
+// wraps to index 0) are never skipped.
+#include <algorithm>
+
+#include "pgb_host.h"
+#include "render.cuh"
+
+namespace pgb {
+namespace {
+
+constexpr int kMaxScenes = 256;
+constexpr int kBatchMaxThreads = 256;
+
+struct BatchArgs {
+  const pgb_scene* scenes;
+  int num_scenes;
+  int clip;
+  const float* origins;
+  const float* dirs;
+  const float* target;
+  const int32_t* ray_scene;
+  int64_t R;
+  float term_thr;
+  int stratified;
+  uint64_t seed;
+  double loss_w;
+  double inv_count;
+  float* rgba_out;
+  float* loss_out;
+  unsigned long long* work;  // ray queue head
+  unsigned* ticket;          // finished blocks
+  double* ray_loss;          // [R] squared error per ray
+};
+
+__device__ __forceinline__ bool brick_clear(const pgb_scene& sc, float nx, float ny, float nz) {
+  if (sc.bricks == nullptr) return false;
+  if (!(nx >= 0.f && ny >= 0.f && nz >= 0.f)) return false;
+  const int fx = (int)floorf(nx), fy = (int)floorf(ny), fz = (int)floorf(nz);
+  if (fx >= sc.dims[0] - 1 || fy >= sc.dims[1] - 1 || fz >= sc.dims[2] - 1) return false;
+  const int L = sc.brick_log2;
+  const uint32_t b = ((uint32_t)(fx >> L) * (uint32_t)sc.brick_dims[1] + (uint32_t)(fy >> L)) *
+                         (uint32_t)sc.brick_dims[2] + (uint32_t)(fz >> L);
+  return ((__ldg(sc.bricks + (b >> 5)) >> (b & 31u)) & 1u) == 0u;
+}
+
+__device__ __forceinline__ uint32_t cell_occupied(const pgb_scene& sc, uint64_t c) {
+  return (__ldg(sc.occupancy + (c >> 5)) >> (uint32_t)(c & 31u)) & 1u;
+}
+
+// Clears the gradient-pass bits of a sample's corners that are not occupied (unoccupied
+// cells are not parameters), in the bit layout of sample_value.
+template <int MODE>
+__device__ __forceinline__ uint32_t occupied_bits(const pgb_scene& sc, const GridP<float>& g,
+                                                  float nx, float ny, float nz, uint32_t bits) {
+  if (sc.occupancy == nullptr || bits == 0u) return bits;
+  if (MODE == PGB_NEAREST) {
+    const uint64_t c = cell_index(g, (int)rintf(nx), (int)rintf(ny), (int)rintf(nz));
+    return cell_occupied(sc, c) ? bits : 0u;
+  }
+  Corners<float> q;
+  trilinear_corners(g, nx, ny, nz, q);
+#pragma unroll
+  for (int corner = 0; corner < 8; ++corner) {
+    const int ix = (corner & 4) ? q.f[0] : q.c[0];
+    const int iy = (corner & 2) ? q.f[1] : q.c[1];
+    const int iz = (corner & 1) ? q.f[2] : q.c[2];
+    if (!cell_occupied(sc, cell_index(g, ix, iy, iz))) bits &= ~(0xfu << (4 * corner));
+  }
+  return bits;
+}
+
+template <typename Store, int MODE, int K>
+__global__ void __launch_bounds__(kBatchMaxThreads) batch_train_kernel(const BatchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pgb_scene* sc_tab = reinterpret_cast<pgb_scene*>(smem_raw);
+  const size_t tab_bytes = ((size_t)a.num_scenes * sizeof(pgb_scene) + 15) & ~(size_t)15;
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(a.scenes);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(smem_raw);
+    const int words = (int)((size_t)a.num_scenes * sizeof(pgb_scene) / 4);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  }
+  __shared__ unsigned s_last;
+  __syncthreads();
+  const int lane = threadIdx.x & (kWarp - 1);
+  const int wib = threadIdx.x >> 5;
+  CoordStage<float, K> cs(smem_raw + tab_bytes, wib);
+
+  for (;;) {
+    unsigned long long rr = 0;
+    if (lane == 0) rr = atomicAdd(a.work, 1ull);
+    rr = __shfl_sync(kFull, rr, 0);
+    if ((int64_t)rr >= a.R) break;
+    const int64_t r = (int64_t)rr;
+    const int sid = a.ray_scene[r];
+    if ((unsigned)sid >= (unsigned)a.num_scenes) {  // not a scene of this batch: no work
+      if (lane == 0) a.ray_loss[r] = 0.0;
+      if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = 0.f;
+      continue;
+    }
+    const pgb_scene& sc = sc_tab[sid];
+
+    // the ray's scene as the single-scene kernels see it
+    RenderArgs<float> ra = {};
+    ra.g.cells = sc.cells;
+    ra.g.X = sc.dims[0]; ra.g.Y = sc.dims[1]; ra.g.Z = sc.dims[2];
+    ra.g.fX = (float)ra.g.X; ra.g.fY = (float)ra.g.Y; ra.g.fZ = (float)ra.g.Z;
+    ra.g.ox = sc.origin[0]; ra.g.oy = sc.origin[1]; ra.g.oz = sc.origin[2];
+    ra.g.pd = sc.points_distance;
+    ra.g.clip = a.clip;
+    ra.S = sc.num_samples;
+    ra.delta = sc.delta_step;
+    ra.stratified = a.stratified;
+    ra.strat_seed = a.seed;
+    float* grad = reinterpret_cast<float*>(sc.grad_cells);
+
+    Ray<float> ray;
+    ray.ox = a.origins[3 * r + 0]; ray.oy = a.origins[3 * r + 1]; ray.oz = a.origins[3 * r + 2];
+    ray.dx = a.dirs[3 * r + 0];    ray.dy = a.dirs[3 * r + 1];    ray.dz = a.dirs[3 * r + 2];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) ray.tgt[c] = a.target[4 * r + c];
+    ray.h = a.stratified ? hash_stream(a.seed, (uint64_t)r) : 0ull;
+
+    const int nchunks = (ra.S + kWarp * K - 1) / (kWarp * K);
+    float v[K][4];
+    uint32_t bits[K];
+    float Ts[K];
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    float T = 1.f, Tstart = 1.f;
+    int last = -1;
+
+    auto gather = [&](int c) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const int s = (c * K + k) * kWarp + lane;
+        v[k][0] = v[k][1] = v[k][2] = v[k][3] = 0.f;
+        bits[k] = 0u;
+        if (s < ra.S) {
+          float nx, ny, nz;
+          sample_coords(ra, ray, s, nx, ny, nz);
+          if (!brick_clear(sc, nx, ny, nz)) {
+            sample_value<float, Store, MODE>(ra.g, nx, ny, nz, v[k], bits[k]);
+            bits[k] = occupied_bits<MODE>(sc, ra.g, nx, ny, nz, bits[k]);
+            cs.put(k, lane, nx, ny, nz);
+          }
+        }
+      }
+    };
+
+    for (int c = 0; c < nchunks; ++c) {
+      if (lane == c) Tstart = T;
+      __syncwarp();
+      gather(c);
+      T = scan_chunk<float, K>(v, T, lane, Ts);
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const float w = v[k][3] * Ts[k];
+        acc[0] += w * v[k][0];
+        acc[1] += w * v[k][1];
+        acc[2] += w * v[k][2];
+        acc[3] += w;
+      }
+      last = c;
+      if (a.term_thr > 0.0f && T < a.term_thr) break;
+    }
+    float px[4];
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) px[ch] = warp_sum(acc[ch]);
+    float gpx[4];
+    double sq = 0.0;
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+      const float diff = px[ch] - ray.tgt[ch];
+      sq += (double)diff * (double)diff;
+      gpx[ch] = (float)(2.0 * a.loss_w * a.inv_count) * diff;
+    }
+    if (lane == 0) a.ray_loss[r] = sq;
+    if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = pick4(px, lane);
+
+    float Snext_carry = 0.f;
+    for (int c = last; c >= 0; --c) {
+      if (c != last) {
+        __syncwarp();
+        gather(c);
+        scan_chunk<float, K>(v, __shfl_sync(kFull, Tstart, c), lane, Ts);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int k = K - 1; k >= 0; --k) {
+        const float al = v[k][3];
+        const float G = gpx[0] * v[k][0] + gpx[1] * v[k][1] + gpx[2] * v[k][2] + gpx[3];
+        float fa = G * al, fb = 1.f - al;
+        warp_suffix_affine(fa, fb, lane);
+        const float S_here = fa + fb * Snext_carry;
+        float S_after = __shfl_down_sync(kFull, S_here, 1);
+        if (lane == kWarp - 1) S_after = Snext_carry;
+        Snext_carry = __shfl_sync(kFull, S_here, 0);
+        if (bits[k] != 0u) {
+          const float w = al * Ts[k];
+          float dv[4] = {gpx[0] * w, gpx[1] * w, gpx[2] * w, Ts[k] * (G - S_after)};
+          float nx, ny, nz;
+          cs.get(k, lane, nx, ny, nz);
+          sample_scatter<float, MODE>(ra.g, grad, nx, ny, nz, dv, bits[k]);
+        }
+      }
+    }
+  }
+
+  // the last block to finish sums the per-ray losses in ray order and resets the queue
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(a.ticket, 1u) == gridDim.x - 1u;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    __shared__ double red[kBatchMaxThreads];
+    double sum = 0.0;
+    for (int64_t i = threadIdx.x; i < a.R; i += blockDim.x) sum += ((volatile double*)a.ray_loss)[i];
+    red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      a.loss_out[0] = (float)(a.loss_w * red[0] * a.inv_count);
+      *a.work = 0ull;
+      *a.ticket = 0u;
+    }
+  }
+}
+
+// --------------------------------------------------------------- brick masks
+__global__ void pack_mask_kernel(const uint8_t* __restrict__ m, int64_t count, uint32_t* __restrict__ out) {
+  const int64_t words = (count + 31) / 32;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t b = 0u;
+    for (int i = 0; i < 32; ++i) {
+      const int64_t c = w * 32 + i;
+      if (c < count && m[c]) b |= 1u << i;
+    }
+    out[w] = b;
+  }
+}
+
+// Dilated brick mask straight from the cell bits: thread b scans the cells of bricks
+// b + {0,1}^3 (2^(L+1) cells per axis, clamped to the grid); a warp ballot assembles 32
+// bricks into one mask word.
+__global__ void build_bricks_kernel(const uint32_t* __restrict__ cell_bits, int X, int Y, int Z,
+                                    int L, int BX, int BY, int BZ, uint32_t* __restrict__ out) {
+  const int64_t NB = (int64_t)BX * BY * BZ;
+  const int64_t words = (NB + 31) / 32;
+  const int lane = threadIdx.x & 31;
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words;
+       w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t b = w * 32 + lane;
+    bool any = false;
+    if (b < NB) {
+      const int bz = (int)(b % BZ);
+      const int64_t bxy = b / BZ;
+      const int by = (int)(bxy % BY), bx = (int)(bxy / BY);
+      const int x0 = bx << L, x1 = min(X, (bx + 2) << L);
+      const int y0 = by << L, y1 = min(Y, (by + 2) << L);
+      const int z0 = bz << L, z1 = min(Z, (bz + 2) << L);  // cells [z0, z1) of each row
+      for (int x = x0; x < x1 && !any; ++x) {
+        for (int y = y0; y < y1 && !any; ++y) {
+          const int64_t c0 = ((int64_t)x * Y + y) * Z + z0, c1 = c0 + (z1 - z0);  // [c0, c1)
+          for (int64_t wd = c0 >> 5; wd <= (c1 - 1) >> 5 && !any; ++wd) {
+            uint32_t m = 0xffffffffu;
+            if (wd == (c0 >> 5)) m &= 0xffffffffu << (c0 & 31);
+            if (wd == ((c1 - 1) >> 5)) m &= 0xffffffffu >> (31 - ((c1 - 1) & 31));
+            any = (__ldg(cell_bits + wd) & m) != 0u;
+          }
+        }
+      }
+    }
+    const uint32_t word = __ballot_sync(0xffffffffu, any);
+    if (lane == 0) out[w] = word;
+  }
+}
+
+__global__ void batch_zero_kernel(const pgb_scene* __restrict__ scenes) {
+  const pgb_scene sc = scenes[blockIdx.y];
+  const int64_t cells = (int64_t)sc.dims[0] * sc.dims[1] * sc.dims[2];  // one float4 per cell
+  uint4* p = reinterpret_cast<uint4*>(sc.grad_cells);
+  if (sc.occupancy == nullptr) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cells;
+         i += (int64_t)gridDim.x * blockDim.x)
+      p[i] = make_uint4(0u, 0u, 0u, 0u);
+    return;
+  }
+  // only occupied cells ever receive gradient: clear those
+  const int64_t words = (cells + 31) / 32;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t bits = __ldg(sc.occupancy + w);
+    while (bits) {
+      const int i = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const int64_t c = w * 32 + i;
+      if (c < cells) p[c] = make_uint4(0u, 0u, 0u, 0u);
+    }
+  }
+}
+
+inline unsigned grid_for(int64_t n, int threads = 256) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 1 << 20));
+}
+
+template <typename Store, int MODE, int K>
+int launch_batch_k(const BatchArgs& a, int threads, cudaStream_t s) {
+  const int warps = threads / kWarp;
+  const size_t tab = (((size_t)a.num_scenes * sizeof(pgb_scene)) + 15) & ~(size_t)15;
+  const size_t smem = tab + (size_t)CoordStage<float, K>::kBytesPerWarp * warps;
+  auto kern = batch_train_kernel<Store, MODE, K>;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static int configured[64] = {0};
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024) != cudaSuccess)
+      return PGB_ERR_LAUNCH;
+    configured[dev] = 1;
+  }
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess ||
+      per_sm < 1)
+    return PGB_ERR_LAUNCH;
+  int64_t blocks = (int64_t)sms * per_sm;
+  blocks = std::min<int64_t>(blocks, (a.R + warps - 1) / warps);
+  blocks = std::max<int64_t>(blocks, 1);
+  kern<<<(unsigned)blocks, threads, smem, s>>>(a);
+  return after_launch();
+}
+
+template <typename Store, int MODE>
+int launch_batch_m(const BatchArgs& a, int K, int threads, cudaStream_t s) {
+  switch (K) {
+    case 2: return launch_batch_k<Store, MODE, 2>(a, threads, s);
+    case 4: return launch_batch_k<Store, MODE, 4>(a, threads, s);
+    case 8: return launch_batch_k<Store, MODE, 8>(a, threads, s);
+    default: return PGB_ERR_ARG;
+  }
+}
+
+}  // namespace
+}  // namespace pgb
+
+using namespace pgb;
+
+extern "C" {
+
+int64_t pgb_batch_workspace_bytes(int64_t num_rays) {
+  return 64 + 8 * std::max<int64_t>(num_rays, 1);
+}
+
+int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, int32_t mode,
+                    int32_t clip, const float* origins, const float* dirs, const float* target,
+                    const int32_t* ray_scene, int64_t num_rays, float term_threshold,
+                    int32_t stratified, uint64_t seed, double loss_weight, float* rgba_out,
+                    float* loss_out, void* workspace, int32_t slots_per_lane,
+                    int32_t threads_per_block, pgb_stream_t stream) {
+  if (!scenes || num_scenes <= 0 || num_scenes > kMaxScenes || num_rays < 0) return PGB_ERR_ARG;
+  if (dtype != PGB_F32 && dtype != PGB_BF16) return PGB_ERR_UNSUPPORTED;
+  if (mode != PGB_NEAREST && mode != PGB_TRILINEAR) return PGB_ERR_ARG;
+  if (!loss_out || !workspace) return PGB_ERR_ARG;
+  if (num_rays > 0 && (!origins || !dirs || !target || !ray_scene)) return PGB_ERR_ARG;
+  if (((uintptr_t)workspace % 16) != 0) return PGB_ERR_ALIGN;
+  const int K = slots_per_lane == 0 ? 2 : slots_per_lane;
+  const int threads = threads_per_block == 0 ? 256 : threads_per_block;
+  if (K != 2 && K != 4 && K != 8) return PGB_ERR_ARG;
+  if (threads != 128 && threads != 256) return PGB_ERR_ARG;
+  BatchArgs a = {};
+  a.scenes = scenes;
+  a.num_scenes = num_scenes;
+  a.clip = clip ? 1 : 0;
+  a.origins = origins;
+  a.dirs = dirs;
+  a.target = target;
+  a.ray_scene = ray_scene;
+  a.R = num_rays;
+  a.term_thr = term_threshold;
+  a.stratified = stratified ? 1 : 0;
+  a.seed = seed;
+  a.loss_w = loss_weight;
+  a.inv_count = num_rays > 0 ? 1.0 / (4.0 * (double)num_rays) : 0.0;
+  a.rgba_out = rgba_out;
+  a.loss_out = loss_out;
+  a.work = reinterpret_cast<unsigned long long*>(workspace);
+  a.ticket = reinterpret_cast<unsigned*>((char*)workspace + 8);
+  a.ray_loss = reinterpret_cast<double*>((char*)workspace + 64);
+  if (dtype == PGB_BF16)
+    return mode == PGB_NEAREST ? launch_batch_m<__nv_bfloat16, PGB_NEAREST>(a, K, threads, stream)
+                               : launch_batch_m<__nv_bfloat16, PGB_TRILINEAR>(a, K, threads, stream);
+  return mode == PGB_NEAREST ? launch_batch_m<float, PGB_NEAREST>(a, K, threads, stream)
+                             : launch_batch_m<float, PGB_TRILINEAR>(a, K, threads, stream);
+}
+
+int pgb_pack_mask(const uint8_t* mask, int64_t count, uint32_t* bits_out, pgb_stream_t stream) {
+  if (count < 0) return PGB_ERR_ARG;
+  if (count == 0) return PGB_OK;
+  if (!mask || !bits_out) return PGB_ERR_ARG;
+  pack_mask_kernel<<<grid_for((count + 31) / 32), 256, 0, stream>>>(mask, count, bits_out);
+  return after_launch();
+}
+
+int pgb_build_bricks(const uint32_t* cell_bits, const int32_t dims[3], int32_t brick_log2,
+                     uint32_t* bricks_out, pgb_stream_t stream) {
+  if (!cell_bits || !dims || !bricks_out || brick_log2 < 0 || brick_log2 > 8) return PGB_ERR_ARG;
+  if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return PGB_ERR_ARG;
+  const int L = brick_log2;
+  const int BX = (dims[0] + (1 << L) - 1) >> L, BY = (dims[1] + (1 << L) - 1) >> L,
+            BZ = (dims[2] + (1 << L) - 1) >> L;
+  const int64_t words = ((int64_t)BX * BY * BZ + 31) / 32;
+  // whole warps per mask word: the grid-stride loop runs over warps
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((words * 32 + 255) / 256, 1 << 16));
+  build_bricks_kernel<<<blocks, 256, 0, stream>>>(cell_bits, dims[0], dims[1], dims[2], L, BX, BY,
+                                                  BZ, bricks_out);
+  return after_launch();
+}
+
+int pgb_batch_zero_grads(const pgb_scene* scenes, int32_t num_scenes, int64_t max_cells,
+                         pgb_stream_t stream) {
+  if (!scenes || num_scenes <= 0 || num_scenes > 65535 || max_cells < 0) return PGB_ERR_ARG;
+  const dim3 grid(std::max(1u, std::min(grid_for(max_cells), 4096u)), (unsigned)num_scenes);
+  batch_zero_kernel<<<grid, 256, 0, stream>>>(scenes);
+  return after_launch();
+}
+
+}  // extern "C"
