@@ -216,6 +216,69 @@ def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup):
             "and gradients, cells stored in this type"}
 
 
+def batched_leg(pg, dev, steps=30, seed=11):
+    """Batched form: 64 scenes (sides from {32,64,128,256}), 5 % occupied cells, BF16
+    cells, rays per scene log-uniform in [1k, 64k], 512 samples per ray, early
+    termination at T < 1e-4, one persistent launch per step replayed from a CUDA graph.
+    Returns aggregate rays/s and per-step latency percentiles."""
+    from plenoxels_gb300.batch import BatchedTrainStep, Scene
+    g = torch.Generator(device=dev).manual_seed(seed)
+    rng = np.random.default_rng(seed)
+    scs, origins, dirs, targets, owners = [], [], [], [], []
+    S = 512
+    for i in range(64):
+        side = int(rng.choice([32, 64, 128, 256]))
+        pd = 3.0 / side
+        ax = (torch.arange(side, device=dev, dtype=torch.float32) - math.ceil(side / 2) + 1) * pd
+        dens = torch.zeros(side, side, side, device=dev)
+        for _ in range(8):
+            c = torch.rand(3, generator=g, device=dev) * 2 - 1
+            a = 5 + 15 * torch.rand((), generator=g, device=dev)
+            d2 = ((ax - c[0]) ** 2)[:, None, None] + ((ax - c[1]) ** 2)[None, :, None] + \
+                ((ax - c[2]) ** 2)[None, None, :]
+            dens += a * torch.exp(-d2 / (2 * 0.3 ** 2))
+        sub = dens.flatten()[torch.randint(0, dens.numel(), (1 << 20,), generator=g, device=dev)]
+        occ = dens > torch.quantile(sub, 0.95)
+        cells = torch.cat([torch.rand(side, side, side, 3, generator=g, device=dev),
+                           dens.unsqueeze(-1)], -1)
+        cells[~occ] = 0.0
+        scs.append(Scene(cells.to(torch.bfloat16).contiguous(), occ, pd, S, 4.0 / S))
+        n = int(round(math.exp(rng.uniform(math.log(1000), math.log(64000)))))
+        per_cam = -(-n // 4)
+        T = torch.from_numpy(scenes.make_cameras(4, seed * 1000 + i)).to(dev)
+        imgs = torch.rand(4, 32, 32, 4, generator=g, device=dev)
+        dd, px = pg.generate_rays_batched(imgs, per_cam, T, 0.691, device=dev)
+        oo = torch.repeat_interleave(T[:, :3, 3], per_cam, 0) + 2.0 * dd
+        origins.append(oo[:n]); dirs.append(dd[:n]); targets.append(px[:n])
+        owners.append(torch.full((n,), i, dtype=torch.int32, device=dev))
+        del dens
+    R = sum(o.shape[0] for o in origins)
+    step = BatchedTrainStep(scs, R, term_threshold=1e-4)
+    step.set_rays(torch.cat(origins), torch.cat(dirs), torch.cat(targets), torch.cat(owners))
+    tiles = step.autotune(reps=3)
+    step.capture()
+    for _ in range(3):
+        step.step()
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        a.record()
+        step.step()
+        b.record()
+    torch.cuda.synchronize(dev)
+    ms = sorted(a.elapsed_time(b) for a, b in ev)
+    p50 = ms[len(ms) // 2]
+    p99 = ms[min(len(ms) - 1, int(math.ceil(0.99 * len(ms))) - 1)]
+    cells = sum(int(sc.cells.shape[0]) ** 3 for sc in scs)
+    occ_cells = sum(int(sc.occupancy.sum()) for sc in scs)
+    return {"value": R / (statistics.median(ms) / 1e3), "unit": "rays/s", "rays_per_step": R,
+            "scenes": len(scs), "cells": cells, "occupied_cells": occ_cells, "samples": S,
+            "p50_ms": p50, "p99_ms": p99, "tiles": {f"K{k}_t{t}": v for (k, t), v in tiles.items()},
+            "chosen_tile": f"K{step.tiles[0]}_t{step.tiles[1]}",
+            "note": "BF16 cells, occupancy-masked fp32 gradients, early termination at T<1e-4, "
+                    "CUDA-graph replay of zeroing + one persistent launch; same rays every step"}
+
+
 def run_reference_arm(args, W):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -252,6 +315,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and torch-GPU legs")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched multi-scene leg")
     args = ap.parse_args()
     W = dict(WORKLOAD)
 
@@ -379,6 +443,9 @@ def main():
             "clocks": clk.summary()}
     line["bf16_storage"] = storage_leg(pg, grid, T, imgs, W, dev, torch.bfloat16, args.steps,
                                        args.warmup)
+    if not args.no_batched:
+        del step
+        line["batched_form"] = batched_leg(pg, dev)
     if not args.no_baselines:
         grid_cpu, T_cpu, imgs_cpu = grid.cpu(), T.cpu(), imgs.cpu()
         line["torch_gpu_baseline"] = torch_gpu_rate(W, grid, T, imgs, dev)
