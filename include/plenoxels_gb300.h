@@ -117,6 +117,20 @@ int pgb_render_train_noalloc(const pgb_grid* grid, const pgb_rays* rays, const v
                              double loss_weight, void* rgba_out, void* grad_cells, void* loss_out,
                              pgb_stream_t stream);
 
+/* pgb_render_train with the reference's extra loss terms (scripts/train.py:156, :170-177):
+ * loss = mse_weight * MSE + beta_weight * mean over all R*S samples of
+ * log(alpha + beta_eps) - log(1 - alpha + beta_eps) (alpha after the clip and the mask).
+ * losses_out[0] receives the weighted MSE and, when beta_weight != 0, losses_out[1] the
+ * weighted beta term (Real). Same workspace as pgb_render_train. */
+typedef struct {
+  double mse_weight;
+  double beta_weight;
+  float beta_eps;
+} pgb_loss_terms;
+int pgb_render_train_terms(const pgb_grid* grid, const pgb_rays* rays, const void* target,
+                           const pgb_loss_terms* terms, void* rgba_out, void* grad_cells,
+                           void* losses_out, void* workspace, pgb_stream_t stream);
+
 /* Debug/parity view of the fused kernels' own index math: for every sample of every
  * ray, the wrapped cell indices the lookup reads (nearest: [R,S,3]; trilinear:
  * [R,S,8,3], corner order of src/grid_functions.py:16-24) and the in-bounds flag
@@ -176,6 +190,28 @@ int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, 
                     int32_t stratified, uint64_t seed, double loss_weight, float* rgba_out,
                     float* loss_out, void* workspace, int32_t slots_per_lane,
                     int32_t threads_per_block, pgb_stream_t stream);
+
+/* ---- optimiser side of the training step (scripts/train.py:44-65, :89, :163-184) ---- */
+
+/* TV sum of squares of a dense fp32 [X,Y,Z,4] grid: sumsq_out[0] (device fp64) = sum over
+ * all axis-neighbour pairs and channels of (v_i - v_j)^2; tv_loss = sqrt(sumsq)
+ * (scripts/train.py:44-65). Deterministic. workspace: pgb_tv_workspace_bytes(), zeroed
+ * once; left zeroed. */
+int64_t pgb_tv_workspace_bytes(void);
+int pgb_tv_sumsq(const float* cells, const int32_t dims[3], double* sumsq_out, void* workspace,
+                 pgb_stream_t stream);
+/* grad += weight / sqrt(sumsq) * sum over neighbours j of (v_i - v_j): the gradient of
+ * weight * sqrt(sumsq) (scripts/train.py:163-165). No-op when sumsq == 0. */
+int pgb_tv_grad(const float* cells, const int32_t dims[3], const double* sumsq, float weight,
+                float* grad_cells, pgb_stream_t stream);
+/* One torch.optim.Adam step (scripts/train.py:89, :182; no weight decay, no amsgrad) over
+ * count fp32 values (count % 4 == 0, 16-byte aligned): exp_avg = lerp(exp_avg, grad,
+ * 1 - beta1), exp_avg_sq = beta2 * exp_avg_sq + (1 - beta2) * grad^2, param -= lr / bc1 *
+ * exp_avg / (sqrt(exp_avg_sq) / sqrt(bc2) + eps), bc_i = 1 - beta_i^step; then
+ * abs_grad_accum += |grad| (scripts/train.py:184, optional) and grad = 0 when zero_grad. */
+int pgb_adam_step(float* param, float* grad, float* exp_avg, float* exp_avg_sq,
+                  float* abs_grad_accum, int64_t count, double lr, double beta1, double beta2,
+                  double eps, int64_t step, int32_t zero_grad, pgb_stream_t stream);
 
 /* ---- drop-in operators, one per reference function ---- */
 

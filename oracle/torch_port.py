@@ -230,3 +230,32 @@ def sample_indices(origins, dirs, num_samples, delta_step, gmin, points_distance
 def jitter_for(seed: int, num_rays: int, num_samples: int, dtype=torch.float32):
     """Stratification offsets j[r, s] of the counter hash."""
     return torch.from_numpy(stratified_jitter(seed, num_rays, num_samples)).to(dtype)
+
+
+# ----------------------------------------------------------------------- training losses
+def tv_loss(grid):
+    """scripts/train.py:44-65: sqrt of the summed squared neighbour differences along
+    the three axes (the reference names them x, y, z but differences dims 1, 2, 0)."""
+    gx = (grid[:, :-1, :, :] - grid[:, 1:, :, :]).pow(2)
+    gy = (grid[:, :, :-1, :] - grid[:, :, 1:, :]).pow(2)
+    gz = (grid[:-1, :, :, :] - grid[1:, :, :, :]).pow(2)
+    return torch.sqrt(gx.sum() + gy.sum() + gz.sum())
+
+
+def beta_loss(alpha, eps=1e-4):
+    """scripts/train.py:170-177 without the weight: mean of log(a + eps) - log(1 - a + eps)
+    over the sampled (masked) opacities."""
+    return (torch.log(alpha + eps) - torch.log(1 - alpha + eps)).mean()
+
+
+def render_samples(grid, origins, dirs, num_samples, delta_step, gmin, points_distance,
+                   mode="nearest", clip=True, jitter=None):
+    """(rgba [R,4], masked sample values [R,S,4]): the path of render() keeping the
+    per-sample values the beta loss reads (scripts/train.py:146-151)."""
+    R = origins.shape[0]
+    pts = sample_positions(origins, dirs, num_samples, delta_step, jitter)
+    n = normalize(pts, gmin, points_distance)
+    g = grid.clip(0, 1) if clip else grid
+    vals, mask, _ = nearest_lookup(n, g) if mode == "nearest" else trilinear_lookup(n, g)
+    vals = (vals * mask.unsqueeze(-1)).reshape(1, R, num_samples, 4)
+    return composite(vals).reshape(R, 4), vals

@@ -76,12 +76,17 @@ class PgbScene(Structure):
     ]
 
 
+class PgbLossTerms(Structure):
+    _fields_ = [("mse_weight", c_double), ("beta_weight", c_double), ("beta_eps", c_float)]
+
+
 _P = c_void_p
 _SIGNATURES = {
     "pgb_render_fwd": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P]),
     "pgb_render_bwd": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P, _P]),
     "pgb_render_train": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, c_double, _P, _P, _P, _P, _P]),
     "pgb_train_workspace_bytes": (c_int64, []),
+    "pgb_render_train_terms": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, POINTER(PgbLossTerms), _P, _P, _P, _P, _P]),
     "pgb_render_train_noalloc": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, c_double, _P, _P, _P, _P]),
     "pgb_render_sample_indices": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P, _P]),
     "pgb_build_bricks": (c_int32, [_P, POINTER(c_int32), c_int32, _P, _P]),
@@ -90,6 +95,11 @@ _SIGNATURES = {
     "pgb_batch_workspace_bytes": (c_int64, [c_int64]),
     "pgb_batch_train": (c_int32, [_P, c_int32, c_int32, c_int32, c_int32, _P, _P, _P, _P, c_int64, c_float,
                                   c_int32, c_uint64, c_double, _P, _P, _P, c_int32, c_int32, _P]),
+    "pgb_tv_workspace_bytes": (c_int64, []),
+    "pgb_tv_sumsq": (c_int32, [_P, POINTER(c_int32), _P, _P, _P]),
+    "pgb_tv_grad": (c_int32, [_P, POINTER(c_int32), _P, c_float, _P, _P]),
+    "pgb_adam_step": (c_int32, [_P, _P, _P, _P, _P, c_int64, c_double, c_double, c_double, c_double,
+                                c_int64, c_int32, _P]),
     "pgb_generate_rays": (c_int32, [_P, c_int32, c_int64, c_float, _P, c_int32, c_int32, _P, c_int32, _P, _P, _P, _P]),
     "pgb_sample_points": (c_int32, [_P, c_int32, c_int64, _P, c_int32, c_float, _P, _P]),
     "pgb_coords_min": (c_int32, [_P, c_int64, _P, _P]),

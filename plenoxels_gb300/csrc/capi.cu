@@ -132,8 +132,13 @@ int dispatch_render<double>(const pgb_grid* g, RenderArgs<double>& a, int phase,
 template <typename Real>
 int render_common(const pgb_grid* g, const pgb_rays* r, int phase, void* rgba_out,
                   const void* d_rgba, const void* target, double loss_w, void* grad,
-                  void* loss_out, void* workspace, cudaStream_t s) {
+                  void* loss_out, void* workspace, cudaStream_t s, double beta_w = 0.0,
+                  float beta_eps = 0.f) {
   RenderArgs<Real> a = render_args<Real>(g, r);
+  a.beta_w = beta_w;
+  a.beta_eps = beta_eps;
+  const double samples = (double)r->num_rays * (double)r->num_samples;
+  a.inv_samples = samples > 0 ? 1.0 / samples : std::nan("");
   a.rgba_out = (Real*)rgba_out;
   a.d_rgba = (const Real*)d_rgba;
   a.target = (const Real*)target;
@@ -141,7 +146,8 @@ int render_common(const pgb_grid* g, const pgb_rays* r, int phase, void* rgba_ou
   a.loss_out = (Real*)loss_out;
   if (workspace) {
     a.partials = (double*)workspace;
-    a.counter = (unsigned*)((char*)workspace + sizeof(double) * kMaxTrainWarps);
+    a.partials_beta = (double*)workspace + kMaxTrainWarps;
+    a.counter = (unsigned*)((char*)workspace + 2 * sizeof(double) * kMaxTrainWarps);
   }
   a.loss_w = loss_w;
   a.inv_count = r->num_rays > 0 ? 1.0 / (4.0 * (double)r->num_rays) : std::nan("");
@@ -184,7 +190,7 @@ int pgb_render_bwd(const pgb_grid* grid, const pgb_rays* rays, const void* d_rgb
 }
 
 int64_t pgb_train_workspace_bytes(void) {
-  return (int64_t)sizeof(double) * kMaxTrainWarps + 256;
+  return (int64_t)2 * sizeof(double) * kMaxTrainWarps + 256;
 }
 
 int pgb_render_train(const pgb_grid* grid, const pgb_rays* rays, const void* target,
@@ -201,6 +207,25 @@ int pgb_render_train(const pgb_grid* grid, const pgb_rays* rays, const void* tar
                                  grad_cells, loss_out, workspace, stream);
   return render_common<float>(grid, rays, kTrain, rgba_out, nullptr, target, loss_weight,
                               grad_cells, loss_out, workspace, stream);
+}
+
+int pgb_render_train_terms(const pgb_grid* grid, const pgb_rays* rays, const void* target,
+                           const pgb_loss_terms* terms, void* rgba_out, void* grad_cells,
+                           void* losses_out, void* workspace, pgb_stream_t stream) {
+  if (!terms) return PGB_ERR_ARG;
+  int st = check_grid(grid);
+  if (st) return st;
+  if ((st = check_rays(grid, rays, true))) return st;
+  if (!grad_cells || !losses_out || !workspace) return PGB_ERR_ARG;
+  if (!rays->cameras && rays->num_rays > 0 && !target) return PGB_ERR_ARG;
+  if (!aligned(grad_cells, 16) || !aligned(workspace, 16)) return PGB_ERR_ALIGN;
+  if (grid->dtype == PGB_F64)
+    return render_common<double>(grid, rays, kTrain, rgba_out, nullptr, target, terms->mse_weight,
+                                 grad_cells, losses_out, workspace, stream, terms->beta_weight,
+                                 terms->beta_eps);
+  return render_common<float>(grid, rays, kTrain, rgba_out, nullptr, target, terms->mse_weight,
+                              grad_cells, losses_out, workspace, stream, terms->beta_weight,
+                              terms->beta_eps);
 }
 
 int pgb_render_sample_indices(const pgb_grid* grid, const pgb_rays* rays, int64_t* index_out,

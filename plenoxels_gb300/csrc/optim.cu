@@ -1,0 +1,211 @@
+// The optimiser side of the reference's training step (scripts/train.py): the TV loss
+// (:44-65, :163-168), Adam (:89, :182) and the |grad| accumulator (:184), as streaming
+// passes over the dense [X,Y,Z,4] grid.
+//
+//  pgb_tv_sumsq  Q = sum over axis-neighbour pairs of (v_i - v_j)^2 (one deterministic
+//                reduction: fp32 per thread over a fixed cell range, fp64 per block, the
+//                last block sums the blocks in order)
+//  pgb_tv_grad   grad += w / sqrt(Q) * sum_{j in N(i)} (v_i - v_j), the gradient of w*sqrt(Q)
+//  pgb_adam_step torch.optim.Adam's update (lerp of the first moment, bias corrections),
+//                accum += |grad|, grad = 0, in one pass
+#include <algorithm>
+#include <cmath>
+
+#include "pgb_host.h"
+#include "pgb_device.cuh"
+
+namespace pgb {
+namespace {
+
+constexpr int kTvThreads = 256;
+constexpr int kTvBlocks = 1024;
+
+__device__ __forceinline__ float sq4(float4 a, float4 b) {
+  const float x = a.x - b.x, y = a.y - b.y, z = a.z - b.z, w = a.w - b.w;
+  return x * x + y * y + z * z + w * w;
+}
+
+__global__ void __launch_bounds__(kTvThreads) tv_sumsq_kernel(const float4* __restrict__ v, int X, int Y,
+                                                              int Z, double* __restrict__ partials,
+                                                              unsigned* __restrict__ counter,
+                                                              double* __restrict__ out) {
+  const int64_t G = (int64_t)X * Y * Z;
+  const int64_t YZ = (int64_t)Y * Z;
+  float acc = 0.f;
+  double acc_d = 0.0;
+  int n = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < G;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % Z);
+    const int64_t ij = i / Z;
+    const int j = (int)(ij % Y);
+    const int x = (int)(ij / Y);
+    const float4 c = __ldg(v + i);
+    if (k + 1 < Z) acc += sq4(c, __ldg(v + i + 1));
+    if (j + 1 < Y) acc += sq4(c, __ldg(v + i + Z));
+    if (x + 1 < X) acc += sq4(c, __ldg(v + i + YZ));
+    if (++n == 64) {  // bound the fp32 run, then fold into fp64
+      acc_d += acc;
+      acc = 0.f;
+      n = 0;
+    }
+  }
+  acc_d += acc;
+  __shared__ double red[kTvThreads];
+  __shared__ bool last;
+  red[threadIdx.x] = acc_d;
+  __syncthreads();
+  for (int w = kTvThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = red[0];
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1u;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double s = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[b];
+    out[0] = s;
+    *counter = 0u;
+  }
+}
+
+__global__ void tv_grad_kernel(const float4* __restrict__ v, int X, int Y, int Z,
+                               const double* __restrict__ sumsq, float weight,
+                               float4* __restrict__ grad) {
+  const double q = sumsq[0];
+  if (!(q > 0.0)) return;  // a constant grid: sqrt is not differentiable at 0
+  const float c = (float)((double)weight / sqrt(q));
+  const int64_t G = (int64_t)X * Y * Z;
+  const int64_t YZ = (int64_t)Y * Z;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < G;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % Z);
+    const int64_t ij = i / Z;
+    const int j = (int)(ij % Y);
+    const int x = (int)(ij / Y);
+    const float4 m = __ldg(v + i);
+    float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto add = [&](float4 nb) {
+      d.x += m.x - nb.x; d.y += m.y - nb.y; d.z += m.z - nb.z; d.w += m.w - nb.w;
+    };
+    if (k > 0) add(__ldg(v + i - 1));
+    if (k + 1 < Z) add(__ldg(v + i + 1));
+    if (j > 0) add(__ldg(v + i - Z));
+    if (j + 1 < Y) add(__ldg(v + i + Z));
+    if (x > 0) add(__ldg(v + i - YZ));
+    if (x + 1 < X) add(__ldg(v + i + YZ));
+    float4 g = grad[i];
+    g.x += c * d.x; g.y += c * d.y; g.z += c * d.z; g.w += c * d.w;
+    grad[i] = g;
+  }
+}
+
+struct AdamConst {
+  float one_minus_b1, b2, one_minus_b2, step_size, inv_bc2_sqrt, eps;
+};
+
+__device__ __forceinline__ float adam_one(float& p, float g, float& m, float& s, const AdamConst& k) {
+  m = m + k.one_minus_b1 * (g - m);        // exp_avg.lerp_(grad, 1 - beta1)
+  s = s * k.b2 + k.one_minus_b2 * g * g;   // exp_avg_sq.mul_(beta2).addcmul_(grad, grad, 1 - beta2)
+  const float denom = sqrtf(s) * k.inv_bc2_sqrt + k.eps;
+  p = p - k.step_size * (m / denom);
+  return fabsf(g);
+}
+
+__global__ void adam_kernel(float4* __restrict__ p, float4* __restrict__ g, float4* __restrict__ m,
+                            float4* __restrict__ s, float4* __restrict__ acc, int64_t n4,
+                            AdamConst k, int zero_grad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float4 P = p[i], Gr = g[i], M = m[i], S = s[i];
+    float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
+    A.x = adam_one(P.x, Gr.x, M.x, S.x, k);
+    A.y = adam_one(P.y, Gr.y, M.y, S.y, k);
+    A.z = adam_one(P.z, Gr.z, M.z, S.z, k);
+    A.w = adam_one(P.w, Gr.w, M.w, S.w, k);
+    p[i] = P;
+    m[i] = M;
+    s[i] = S;
+    if (acc) {
+      float4 a = acc[i];
+      a.x += A.x; a.y += A.y; a.z += A.z; a.w += A.w;
+      acc[i] = a;
+    }
+    if (zero_grad) g[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+inline unsigned stream_blocks(int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+}
+
+inline bool al16(const void* p) { return ((uintptr_t)p % 16) == 0; }
+
+}  // namespace
+}  // namespace pgb
+
+using namespace pgb;
+
+extern "C" {
+
+int64_t pgb_tv_workspace_bytes(void) { return (int64_t)sizeof(double) * kTvBlocks + 256; }
+
+int pgb_tv_sumsq(const float* cells, const int32_t dims[3], double* sumsq_out, void* workspace,
+                 pgb_stream_t stream) {
+  if (!cells || !dims || !sumsq_out || !workspace) return PGB_ERR_ARG;
+  if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return PGB_ERR_ARG;
+  if (!al16(cells) || !al16(workspace)) return PGB_ERR_ALIGN;
+  const int64_t G = (int64_t)dims[0] * dims[1] * dims[2];
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((G + kTvThreads - 1) / kTvThreads, kTvBlocks));
+  tv_sumsq_kernel<<<blocks, kTvThreads, 0, stream>>>(
+      reinterpret_cast<const float4*>(cells), dims[0], dims[1], dims[2], (double*)workspace,
+      (unsigned*)((char*)workspace + sizeof(double) * kTvBlocks), sumsq_out);
+  return after_launch();
+}
+
+int pgb_tv_grad(const float* cells, const int32_t dims[3], const double* sumsq, float weight,
+                float* grad_cells, pgb_stream_t stream) {
+  if (!cells || !dims || !sumsq || !grad_cells) return PGB_ERR_ARG;
+  if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return PGB_ERR_ARG;
+  if (!al16(cells) || !al16(grad_cells)) return PGB_ERR_ALIGN;
+  const int64_t G = (int64_t)dims[0] * dims[1] * dims[2];
+  tv_grad_kernel<<<stream_blocks(G), 256, 0, stream>>>(reinterpret_cast<const float4*>(cells), dims[0],
+                                                       dims[1], dims[2], sumsq, weight,
+                                                       reinterpret_cast<float4*>(grad_cells));
+  return after_launch();
+}
+
+int pgb_adam_step(float* param, float* grad, float* exp_avg, float* exp_avg_sq, float* abs_grad_accum,
+                  int64_t count, double lr, double beta1, double beta2, double eps, int64_t step,
+                  int32_t zero_grad, pgb_stream_t stream) {
+  if (count < 0 || step < 1) return PGB_ERR_ARG;
+  if (count == 0) return PGB_OK;
+  if (!param || !grad || !exp_avg || !exp_avg_sq) return PGB_ERR_ARG;
+  if (count % 4 != 0) return PGB_ERR_UNSUPPORTED;
+  if (!al16(param) || !al16(grad) || !al16(exp_avg) || !al16(exp_avg_sq) ||
+      (abs_grad_accum && !al16(abs_grad_accum)))
+    return PGB_ERR_ALIGN;
+  // torch.optim.Adam (non-capturable path): bias corrections in double on the host
+  const double bc1 = 1.0 - std::pow(beta1, (double)step);
+  const double bc2 = 1.0 - std::pow(beta2, (double)step);
+  AdamConst k;
+  k.one_minus_b1 = (float)(1.0 - beta1);
+  k.b2 = (float)beta2;
+  k.one_minus_b2 = (float)(1.0 - beta2);
+  k.step_size = (float)(lr / bc1);
+  k.inv_bc2_sqrt = (float)(1.0 / std::sqrt(bc2));
+  k.eps = (float)eps;
+  const int64_t n4 = count / 4;
+  adam_kernel<<<stream_blocks(n4), 256, 0, stream>>>(
+      reinterpret_cast<float4*>(param), reinterpret_cast<float4*>(grad),
+      reinterpret_cast<float4*>(exp_avg), reinterpret_cast<float4*>(exp_avg_sq),
+      reinterpret_cast<float4*>(abs_grad_accum), n4, k, zero_grad ? 1 : 0);
+  return after_launch();
+}
+
+}  // extern "C"

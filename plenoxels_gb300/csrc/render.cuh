@@ -69,6 +69,12 @@ struct RenderArgs {
   unsigned* counter;
   double loss_w;
   double inv_count;
+  // beta loss of scripts/train.py:170-177: beta_w * mean over all R*S samples of
+  // log(alpha + eps) - log(1 - alpha + eps) (0: off)
+  double beta_w;
+  float beta_eps;
+  double inv_samples;
+  double* partials_beta;
 };
 
 template <typename Real>
@@ -402,7 +408,10 @@ render_kernel(const RenderArgs<Real> a) {
   const int nchunks = (a.S + kWarp * K - 1) / (kWarp * K);
   CoordStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
   double loss_lane = 0.0;
+  double beta_lane = 0.0;
+  const bool with_beta = PHASE == kTrain && a.beta_w != 0.0;
   __shared__ double s_part[32];  // per-warp loss partials (training phase)
+  __shared__ double s_part_beta[32];
   __shared__ unsigned s_done;    // warps of this block that finished (training phase)
   if (PHASE == kTrain) {
     if (threadIdx.x == 0) s_done = 0u;
@@ -432,6 +441,15 @@ render_kernel(const RenderArgs<Real> a) {
         acc[1] += w * v[k][1];
         acc[2] += w * v[k][2];
         acc[3] += w;
+      }
+      if (with_beta) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          if ((c * K + k) * kWarp + lane < a.S) {
+            const Real al = v[k][3], e = (Real)a.beta_eps;
+            beta_lane += (double)(log(al + e) - log(Real(1) - al + e));
+          }
+        }
       }
       last = c;
       if (a.term_thr > 0.0f && T < (Real)a.term_thr) break;
@@ -487,6 +505,10 @@ render_kernel(const RenderArgs<Real> a) {
           dv[1] = gpx[1] * w;
           dv[2] = gpx[2] * w;
           dv[3] = Ts[k] * (G - S_after);
+          if (with_beta) {
+            const Real e = (Real)a.beta_eps;
+            dv[3] += (Real)(a.beta_w * a.inv_samples) * (Real(1) / (al + e) + Real(1) / (Real(1) - al + e));
+          }
           Real nx, ny, nz;
           if (PGB_COORDS_IN_SMEM) {
             cs.get(k, lane, nx, ny, nz);
@@ -505,8 +527,10 @@ render_kernel(const RenderArgs<Real> a) {
     // the last block sums the blocks in block order
     const int wib = threadIdx.x >> 5;
     unsigned last_warp = 0;
+    beta_lane = warp_sum(beta_lane);
     if (lane == 0) {
       s_part[wib] = loss_lane;
+      s_part_beta[wib] = beta_lane;
       __threadfence_block();
       last_warp = atomicAdd(&s_done, 1u) == (unsigned)warps_per_block - 1u;
     }
@@ -515,20 +539,29 @@ render_kernel(const RenderArgs<Real> a) {
       unsigned last_block = 0;
       if (lane == 0) {
         __threadfence_block();
-        double sum = 0.0;
-        for (int i = 0; i < warps_per_block; ++i) sum += ((volatile double*)s_part)[i];
+        double sum = 0.0, bsum = 0.0;
+        for (int i = 0; i < warps_per_block; ++i) {
+          sum += ((volatile double*)s_part)[i];
+          bsum += ((volatile double*)s_part_beta)[i];
+        }
         a.partials[blockIdx.x] = sum;
+        if (with_beta) a.partials_beta[blockIdx.x] = bsum;
         __threadfence();
         last_block = atomicAdd(a.counter, 1u) == gridDim.x - 1u;
       }
       last_block = __shfl_sync(kFull, last_block, 0);
       if (last_block) {
         __threadfence();
-        double sum = 0.0;
-        for (unsigned i = lane; i < gridDim.x; i += kWarp) sum += *((volatile double*)a.partials + i);
+        double sum = 0.0, bsum = 0.0;
+        for (unsigned i = lane; i < gridDim.x; i += kWarp) {
+          sum += *((volatile double*)a.partials + i);
+          if (with_beta) bsum += *((volatile double*)a.partials_beta + i);
+        }
         sum = warp_sum(sum);
+        bsum = warp_sum(bsum);
         if (lane == 0) {
           a.loss_out[0] = (Real)(a.loss_w * sum * a.inv_count);
+          if (with_beta) a.loss_out[1] = (Real)(a.beta_w * bsum * a.inv_samples);
           *a.counter = 0u;
         }
       }

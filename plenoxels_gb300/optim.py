@@ -1,0 +1,57 @@
+"""The optimiser side of the reference's training step (scripts/train.py) for one dense
+fp32 grid: torch.optim.Adam (:89, :182), the TV loss (:44-65, :163-168) and the |grad|
+accumulator (:184), as streaming kernels that also clear the gradient for the next step.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from ._lib import check, ptr, require_cuda
+
+
+class FusedAdam:
+    """torch.optim.Adam (no weight decay, no amsgrad) over one dense [X,Y,Z,4] fp32 grid.
+
+    step(grad) applies one update from grad, adds |grad| to ``abs_grad`` (the reference's
+    ``grid_cells_full_grad``) and zeroes grad, all in one pass, so the next training
+    step can accumulate into grad without a separate fill."""
+
+    def __init__(self, grid, lr, betas=(0.9, 0.999), eps=1e-8, accumulate_abs_grad=True):
+        require_cuda(grid)
+        if grid.dtype != torch.float32 or not grid.is_contiguous() or grid.numel() % 4 != 0:
+            raise TypeError("FusedAdam takes a contiguous float32 grid")
+        self.grid = grid
+        self.lr = float(lr)
+        self.betas = (float(betas[0]), float(betas[1]))
+        self.eps = float(eps)
+        self.exp_avg = torch.zeros_like(grid)
+        self.exp_avg_sq = torch.zeros_like(grid)
+        self.abs_grad = torch.zeros_like(grid) if accumulate_abs_grad else None
+        self.step_count = 0
+        lib = _lib.load()
+        self._tv_ws = torch.zeros(lib.pgb_tv_workspace_bytes(), dtype=torch.uint8, device=grid.device)
+        self.tv_sumsq = torch.zeros((), dtype=torch.float64, device=grid.device)
+
+    def add_tv(self, grad, weight):
+        """Adds the gradient of weight * tv_loss(grid) (scripts/train.py:163-165) to grad;
+        returns the term's value as a device scalar."""
+        lib = _lib.load()
+        s = torch.cuda.current_stream(self.grid.device).cuda_stream
+        dims = _lib.dims3(self.grid.shape)
+        check(lib.pgb_tv_sumsq(ptr(self.grid), dims, ptr(self.tv_sumsq), ptr(self._tv_ws), s), "tv loss")
+        check(lib.pgb_tv_grad(ptr(self.grid), dims, ptr(self.tv_sumsq), float(weight), ptr(grad), s),
+              "tv loss")
+        return float(weight) * self.tv_sumsq.sqrt()
+
+    @torch.no_grad()
+    def step(self, grad=None, zero_grad=True):
+        grad = self.grid.grad if grad is None else grad
+        if grad is None or grad.shape != self.grid.shape or grad.dtype != torch.float32:
+            raise ValueError("step needs the grid's float32 gradient")
+        self.step_count += 1
+        s = torch.cuda.current_stream(self.grid.device).cuda_stream
+        check(_lib.load().pgb_adam_step(ptr(self.grid), ptr(grad), ptr(self.exp_avg),
+                                        ptr(self.exp_avg_sq), ptr(self.abs_grad), self.grid.numel(),
+                                        self.lr, self.betas[0], self.betas[1], self.eps,
+                                        self.step_count, 1 if zero_grad else 0, s), "adam step")

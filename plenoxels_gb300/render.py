@@ -163,6 +163,9 @@ def camera_sample_indices(grid, transforms, images, camera_angle_x, num_rays, ra
 class FusedTrainStep:
     """Forward, MSE loss and backward of a batch of rays in one kernel launch.
 
+    beta > 0 adds the reference's beta loss on the sampled opacities (scripts/train.py:
+    170-177) in the same launch; ``self.losses`` holds [weighted MSE, beta term].
+
     The gradient goes to ``self.grad`` (fp32 for fp32/bf16 grids, fp64 for fp64 grids),
     which is also attached as ``grid.grad`` when the dtypes agree, so a torch optimizer
     can step on it. Each call zeroes the gradient first (optimizer.zero_grad semantics)
@@ -177,7 +180,7 @@ class FusedTrainStep:
 
     def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
                  grid_min=None, clip=True, stratified=False, seed=0, term_threshold=0.0,
-                 loss_weight=1.0, overlap_zero=False):
+                 loss_weight=1.0, overlap_zero=False, beta=0.0, beta_eps=1e-4):
         require_cuda(grid)
         if grid.dim() != 4 or grid.shape[-1] != 4 or not grid.is_contiguous():
             raise ValueError("grid must be a contiguous [X,Y,Z,4] tensor")
@@ -194,6 +197,8 @@ class FusedTrainStep:
         self.seed = int(seed)
         self.term_threshold = float(term_threshold)
         self.loss_weight = float(loss_weight)
+        self.beta = float(beta)
+        self.beta_eps = float(beta_eps)
         lib = _lib.load()
         dev = grid.device
         self.workspace = torch.zeros(lib.pgb_train_workspace_bytes(), dtype=torch.uint8, device=dev)
@@ -205,7 +210,9 @@ class FusedTrainStep:
             self._zeroed = [None, None]  # event: buffer b is zero and free
         self._cur = 0
         self.grad = self._grads[0]
-        self.loss = torch.zeros((), dtype=self.real, device=dev)
+        # losses[0]: loss_weight * MSE; losses[1]: the beta term (scripts/train.py:170-177)
+        self.losses = torch.zeros(2, dtype=self.real, device=dev)
+        self.loss = self.losses[0]
         self._attach()
         self._cams = None
         self.kernel_events = None  # list of (start, end) CUDA events, when timing is wanted
@@ -255,9 +262,15 @@ class FusedTrainStep:
         if self.kernel_events is not None:
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record(stream)
-        check(lib.pgb_render_train(gdesc, rdesc, ptr(target), self.loss_weight, ptr(rgba_out),
-                                   ptr(grad), ptr(self.loss), ptr(self.workspace),
-                                   stream.cuda_stream), "train step")
+        if self.beta == 0.0:
+            check(lib.pgb_render_train(gdesc, rdesc, ptr(target), self.loss_weight, ptr(rgba_out),
+                                       ptr(grad), ptr(self.losses), ptr(self.workspace),
+                                       stream.cuda_stream), "train step")
+        else:
+            terms = _lib.PgbLossTerms(self.loss_weight, self.beta, self.beta_eps)
+            check(lib.pgb_render_train_terms(gdesc, rdesc, ptr(target), terms, ptr(rgba_out),
+                                             ptr(grad), ptr(self.losses), ptr(self.workspace),
+                                             stream.cuda_stream), "train step")
         if ev is not None:
             ev[1].record(stream)
             self.kernel_events.append(ev)
