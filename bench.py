@@ -216,7 +216,7 @@ def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup):
             "and gradients, cells stored in this type"}
 
 
-def batched_leg(pg, dev, steps=30, seed=11):
+def batched_leg(pg, dev, steps=30, seed=11, num_scenes=64):
     """Batched form: 64 scenes (sides from {32,64,128,256}), 5 % occupied cells, BF16
     cells, rays per scene log-uniform in [1k, 64k], 512 samples per ray, early
     termination at T < 1e-4, one persistent launch per step replayed from a CUDA graph.
@@ -226,7 +226,7 @@ def batched_leg(pg, dev, steps=30, seed=11):
     rng = np.random.default_rng(seed)
     scs, origins, dirs, targets, owners = [], [], [], [], []
     S = 512
-    for i in range(64):
+    for i in range(num_scenes):
         side = int(rng.choice([32, 64, 128, 256]))
         pd = 3.0 / side
         ax = (torch.arange(side, device=dev, dtype=torch.float32) - math.ceil(side / 2) + 1) * pd
@@ -279,6 +279,44 @@ def batched_leg(pg, dev, steps=30, seed=11):
                     "CUDA-graph replay of zeroing + one persistent launch; same rays every step"}
 
 
+def full_step_leg(pg, grid, T, imgs, W, dev, steps, warmup):
+    """The whole reference training step (scripts/train.py:142-184) at its default weights
+    (lr 0.0075, tv 1e-5, beta 5e-3): fused render + MSE + beta + backward, TV gradient,
+    Adam + |grad| accumulator + gradient clear. Also the Adam pass's achieved bandwidth."""
+    from plenoxels_gb300.train import Trainer
+    S, R = W["samples"], W["rays"]
+    g = grid.clone()
+    tr = Trainer(g, 3.0 / W["grid"], S, (W["far"] - W["near"]) / S, 0.0075, tv=1e-5, beta=5e-3,
+                 mode=W["mode"], stratified=True, seed=7)
+    stream = torch.cuda.current_stream(dev)
+    for i in range(warmup):
+        tr.step_cameras(T, imgs, W["camera_angle_x"], R, 7000 + i, near=W["near"])
+    torch.cuda.synchronize(dev)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for i in range(steps):
+        tr.step_cameras(T, imgs, W["camera_angle_x"], R, 8000 + i, near=W["near"])
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = t0.elapsed_time(t1) / steps
+    # the Adam pass alone: reads param, grad, both moments and the accumulator, writes all
+    # five back (the gradient as zeros): 10 x 16 B per cell
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    for _ in range(steps):
+        tr.opt.step(tr.render.grad)
+    a1.record(stream)
+    torch.cuda.synchronize(dev)
+    adam_ms = a0.elapsed_time(a1) / steps
+    adam_bytes = grid.numel() // 4 * 160
+    peak, _ = _peaks()
+    return {"value": R / (ms / 1e3), "unit": "rays/s", "ms_per_step": ms,
+            "adam_ms": adam_ms, "adam_gbs": adam_bytes / (adam_ms / 1e3) / 1e9,
+            "adam_frac_of_measured_peak": adam_bytes / (adam_ms / 1e3) / 1e9 / peak,
+            "note": "render + MSE + beta (5e-3) + backward, TV (1e-5) gradient, Adam (lr 0.0075) "
+                    "with |grad| accumulation; dense fp32 grid of 256^3"}
+
+
 def run_reference_arm(args, W):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -316,6 +354,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and torch-GPU legs")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched multi-scene leg")
+    ap.add_argument("--batched-only", action="store_true", help="run only the batched leg")
+    ap.add_argument("--batched-scenes", type=int, default=64, help="scenes of the batched leg")
     args = ap.parse_args()
     W = dict(WORKLOAD)
 
@@ -325,6 +365,12 @@ def main():
 
     import plenoxels_gb300 as pg
     import plenoxels_gb300.render  # noqa: F401
+
+    if args.batched_only:
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        torch.cuda.set_device(dev)
+        print(json.dumps({"batched_form": batched_leg(pg, dev, num_scenes=args.batched_scenes)}))
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -443,6 +489,7 @@ def main():
             "clocks": clk.summary()}
     line["bf16_storage"] = storage_leg(pg, grid, T, imgs, W, dev, torch.bfloat16, args.steps,
                                        args.warmup)
+    line["full_training_step"] = full_step_leg(pg, grid, T, imgs, W, dev, args.steps, args.warmup)
     if not args.no_batched:
         del step
         line["batched_form"] = batched_leg(pg, dev)

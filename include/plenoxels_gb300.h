@@ -49,6 +49,8 @@ typedef struct {
   double points_distance;   /* cell pitch, held exactly in "Real" */
   int32_t clip;             /* 1: clamp cell values to [0,1] at lookup (scripts/train.py:146) */
   int32_t mode;             /* PGB_NEAREST | PGB_TRILINEAR */
+  float alpha_floor;        /* >0: after the clamp, alpha below this reads as 0 (the inference
+                               threshold of src/visualization.py:117-119); 0 for training */
 } pgb_grid;
 
 /* Cameras for in-kernel ray generation (src/ray_sampling.py:195-264). */
@@ -213,6 +215,19 @@ int pgb_adam_step(float* param, float* grad, float* exp_avg, float* exp_avg_sq,
                   float* abs_grad_accum, int64_t count, double lr, double beta1, double beta2,
                   double eps, int64_t step, int32_t zero_grad, pgb_stream_t stream);
 
+/* src/grid_functions.py:173-181 average_pool3d_grid (scripts/train.py:108-123): average of
+ * a cubic window of `window` cells, stride `stride`, no padding, of a contiguous fp32
+ * [X,Y,Z,4] grid into [Xo,Yo,Zo,4], Xo = (X - window) / stride + 1. pgb_avg_pool3d_shape
+ * gives the output dims and the scratch bytes both directions need (caller-provided). */
+int pgb_avg_pool3d_shape(const int32_t dims[3], int32_t window, int32_t stride,
+                         int32_t out_dims[3], int64_t* scratch_bytes);
+int pgb_avg_pool3d_fwd(const float* cells, const int32_t dims[3], int32_t window, int32_t stride,
+                       void* scratch, float* out, pgb_stream_t stream);
+/* Adjoint: d_cells[X,Y,Z,4] = the pooled gradient spread back over each window (every cell
+ * written, so no prior zeroing is needed). */
+int pgb_avg_pool3d_bwd(const float* d_out, const int32_t dims[3], int32_t window, int32_t stride,
+                       void* scratch, float* d_cells, pgb_stream_t stream);
+
 /* ---- drop-in operators, one per reference function ---- */
 
 /* src/ray_sampling.py:195-264 generate_rays_batched. uv: [C*Rc,2] uniforms in [0,1)
@@ -298,6 +313,11 @@ int pgb_composite_bwd(const void* samples, int32_t dtype, int64_t num_rays, int3
                       const void* d_out, void* d_samples, pgb_stream_t stream);
 
 /* ---- utilities ---- */
+
+/* Image of the premultiplied RGBA of res x res even-spread rays (src/visualization.py:
+ * 147-152): u8 = clip(round_half_even(255 * rgba), 0, 255), stored transposed, so
+ * image_out[a][b] is ray b * res + a. */
+int pgb_rgba_to_image(const float* rgba, int32_t res, uint8_t* image_out, pgb_stream_t stream);
 
 /* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel. */
 int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream);

@@ -259,3 +259,10 @@ def render_samples(grid, origins, dirs, num_samples, delta_step, gmin, points_di
     vals, mask, _ = nearest_lookup(n, g) if mode == "nearest" else trilinear_lookup(n, g)
     vals = (vals * mask.unsqueeze(-1)).reshape(1, R, num_samples, 4)
     return composite(vals).reshape(R, 4), vals
+
+
+def average_pool3d_grid(tensor, receptive_field_size=3, stride=None):
+    """src/grid_functions.py:173-181: avg_pool3d of the channels-last grid."""
+    x = tensor.permute(3, 0, 1, 2).unsqueeze(0)
+    r = (receptive_field_size,) * 3
+    return torch.nn.functional.avg_pool3d(x, r, stride=stride).squeeze(0).permute(1, 2, 3, 0)

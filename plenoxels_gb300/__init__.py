@@ -7,7 +7,7 @@ through the C ABI of ``libplenoxels_gb300.so`` (include/plenoxels_gb300.h). The 
 entry points (``render_rays``, ``FusedTrainStep``) run the whole path in one launch.
 """
 from . import _lib
-from .grid_functions import (collect_cell_information_via_indices, find_out_of_bound,
+from .grid_functions import (average_pool3d_grid, collect_cell_information_via_indices, find_out_of_bound,
                              fix_out_of_bounds, generate_grid, get_grid_points_indices,
                              get_nearest_voxels, grid_origin, trilinear_interpolation)
 from .ray_sampling import (compute_alpha_weighted_pixels, generate_rays_batched,
@@ -17,6 +17,7 @@ from .render import FusedTrainStep, render_rays, render_sample_indices
 __all__ = [
     "generate_grid", "grid_origin", "get_nearest_voxels", "find_out_of_bound", "fix_out_of_bounds",
     "get_grid_points_indices", "collect_cell_information_via_indices", "trilinear_interpolation",
+    "average_pool3d_grid",
     "normalize_samples_for_indecies", "generate_rays_batched", "sample_camera_rays_batched",
     "compute_alpha_weighted_pixels", "render_rays", "render_sample_indices", "FusedTrainStep",
     "load_library", "launch_count",

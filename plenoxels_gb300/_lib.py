@@ -30,6 +30,7 @@ class PgbGrid(Structure):
         ("points_distance", c_double),
         ("clip", c_int32),
         ("mode", c_int32),
+        ("alpha_floor", c_float),
     ]
 
 
@@ -100,6 +101,9 @@ _SIGNATURES = {
     "pgb_tv_grad": (c_int32, [_P, POINTER(c_int32), _P, c_float, _P, _P]),
     "pgb_adam_step": (c_int32, [_P, _P, _P, _P, _P, c_int64, c_double, c_double, c_double, c_double,
                                 c_int64, c_int32, _P]),
+    "pgb_avg_pool3d_shape": (c_int32, [POINTER(c_int32), c_int32, c_int32, POINTER(c_int32), POINTER(c_int64)]),
+    "pgb_avg_pool3d_fwd": (c_int32, [_P, POINTER(c_int32), c_int32, c_int32, _P, _P, _P]),
+    "pgb_avg_pool3d_bwd": (c_int32, [_P, POINTER(c_int32), c_int32, c_int32, _P, _P, _P]),
     "pgb_generate_rays": (c_int32, [_P, c_int32, c_int64, c_float, _P, c_int32, c_int32, _P, c_int32, _P, _P, _P, _P]),
     "pgb_sample_points": (c_int32, [_P, c_int32, c_int64, _P, c_int32, c_float, _P, _P]),
     "pgb_coords_min": (c_int32, [_P, c_int64, _P, _P]),
@@ -117,6 +121,7 @@ _SIGNATURES = {
     "pgb_composite_fwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P]),
     "pgb_composite_bwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P, _P]),
     "pgb_fill_zero": (c_int32, [_P, c_int64, _P]),
+    "pgb_rgba_to_image": (c_int32, [_P, c_int32, _P, _P]),
     "pgb_hash_uniform": (c_float, [c_uint64, c_uint64, c_uint32]),
     "pgb_launch_count": (c_int64, []),
     "pgb_version": (c_char_p, []),
@@ -186,7 +191,8 @@ def real_dtype(storage: torch.dtype) -> torch.dtype:
     return torch.float64 if storage == torch.float64 else torch.float32
 
 
-def make_grid(cells: torch.Tensor, origin, points_distance: float, mode: int, clip: bool) -> PgbGrid:
+def make_grid(cells: torch.Tensor, origin, points_distance: float, mode: int, clip: bool,
+              alpha_floor: float = 0.0) -> PgbGrid:
     if cells.dim() != 4 or cells.shape[-1] != 4:
         raise ValueError(f"grid must be [X,Y,Z,4], got {tuple(cells.shape)}")
     if cells.dtype not in STORAGE_CODES:
@@ -202,6 +208,7 @@ def make_grid(cells: torch.Tensor, origin, points_distance: float, mode: int, cl
     g.points_distance = float(points_distance)
     g.clip = 1 if clip else 0
     g.mode = mode
+    g.alpha_floor = float(alpha_floor)
     return g
 
 

@@ -43,6 +43,7 @@ int composite_max_samples();
 int op_render_indices_f32(const RenderArgs<float>&, int, int64_t*, uint8_t*, cudaStream_t);
 int op_render_indices_f64(const RenderArgs<double>&, int, int64_t*, uint8_t*, cudaStream_t);
 int op_fill_zero(void*, int64_t, cudaStream_t);
+int op_rgba_to_image(const float*, int, uint8_t*, cudaStream_t);
 
 namespace {
 
@@ -69,6 +70,7 @@ GridP<Real> grid_params(const pgb_grid* g) {
   p.ox = (Real)g->origin[0]; p.oy = (Real)g->origin[1]; p.oz = (Real)g->origin[2];
   p.pd = (Real)g->points_distance;
   p.clip = g->clip ? 1 : 0;
+  p.alpha_floor = g->alpha_floor;
   return p;
 }
 
@@ -431,6 +433,13 @@ int pgb_composite_bwd(const void* samples, int32_t dtype, int64_t num_rays, int3
   if (!samples || !d_out || !d_samples) return PGB_ERR_ARG;
   if (!aligned(samples, 16)) return PGB_ERR_ALIGN;
   return op_composite(samples, dtype == PGB_F64, num_rays, num_samples, d_out, d_samples, 1, stream);
+}
+
+int pgb_rgba_to_image(const float* rgba, int32_t res, uint8_t* image_out, pgb_stream_t stream) {
+  if (res < 0) return PGB_ERR_ARG;
+  if (res == 0) return PGB_OK;
+  if (!rgba || !image_out) return PGB_ERR_ARG;
+  return op_rgba_to_image(rgba, res, image_out, stream);
 }
 
 int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream) {

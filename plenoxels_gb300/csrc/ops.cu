@@ -552,6 +552,20 @@ __global__ void render_indices_kernel(const RenderArgs<Real> a, int64_t* __restr
   }
 }
 
+// (255 * rgba).round().clip(0, 255) as uint8, written transposed (src/visualization.py:148-152)
+__global__ void rgba_to_image_kernel(const float* __restrict__ rgba, int res, uint8_t* __restrict__ out) {
+  const int64_t n = (int64_t)res * res;
+  PGB_FOR(i, n) {
+    const int64_t a = i / res, b = i - a * res;  // out[a][b] = ray b * res + a
+    const float* p = rgba + 4 * (b * res + a);
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+      const float v = fminf(fmaxf(rintf(rmul(p[ch], 255.0f)), 0.0f), 255.0f);
+      out[4 * i + ch] = (uint8_t)v;
+    }
+  }
+}
+
 __global__ void fill_zero_kernel(uint4* __restrict__ p, int64_t n16, uint8_t* __restrict__ tail,
                                  int tail_bytes) {
   PGB_FOR(i, n16) p[i] = make_uint4(0u, 0u, 0u, 0u);
@@ -751,6 +765,11 @@ int op_render_indices_f32(const RenderArgs<float>& a, int mode, int64_t* idx, ui
 }
 int op_render_indices_f64(const RenderArgs<double>& a, int mode, int64_t* idx, uint8_t* inb, cudaStream_t s) {
   return render_indices_t(a, mode, idx, inb, s);
+}
+
+int op_rgba_to_image(const float* rgba, int res, uint8_t* out, cudaStream_t s) {
+  rgba_to_image_kernel<<<blocks_for((int64_t)res * res), kThreads, 0, s>>>(rgba, res, out);
+  return after_launch();
 }
 
 int op_fill_zero(void* p, int64_t bytes, cudaStream_t s) {

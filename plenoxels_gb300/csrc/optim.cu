@@ -18,39 +18,42 @@ namespace pgb {
 namespace {
 
 constexpr int kTvThreads = 256;
-constexpr int kTvBlocks = 1024;
+constexpr int kTvMaxBlocks = 1 << 18;
 
 __device__ __forceinline__ float sq4(float4 a, float4 b) {
   const float x = a.x - b.x, y = a.y - b.y, z = a.z - b.z, w = a.w - b.w;
   return x * x + y * y + z * z + w * w;
 }
 
+// Block (bz, y, xc) covers z in [bz*T, bz*T + T) of row y for the x values x = xc, xc + XC,
+// ...: no integer division per cell, coalesced along z.
+constexpr int kTvXChunks = 8;
+
 __global__ void __launch_bounds__(kTvThreads) tv_sumsq_kernel(const float4* __restrict__ v, int X, int Y,
                                                               int Z, double* __restrict__ partials,
                                                               unsigned* __restrict__ counter,
                                                               double* __restrict__ out) {
-  const int64_t G = (int64_t)X * Y * Z;
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
   const int64_t YZ = (int64_t)Y * Z;
-  float acc = 0.f;
   double acc_d = 0.0;
-  int n = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < G;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(i % Z);
-    const int64_t ij = i / Z;
-    const int j = (int)(ij % Y);
-    const int x = (int)(ij / Y);
-    const float4 c = __ldg(v + i);
-    if (k + 1 < Z) acc += sq4(c, __ldg(v + i + 1));
-    if (j + 1 < Y) acc += sq4(c, __ldg(v + i + Z));
-    if (x + 1 < X) acc += sq4(c, __ldg(v + i + YZ));
-    if (++n == 64) {  // bound the fp32 run, then fold into fp64
-      acc_d += acc;
-      acc = 0.f;
-      n = 0;
+  if (z < Z) {
+    float acc = 0.f;
+    int n = 0;
+    for (int x = blockIdx.z; x < X; x += gridDim.z) {
+      const int64_t i = (int64_t)x * YZ + (int64_t)y * Z + z;
+      const float4 c = __ldg(v + i);
+      if (z + 1 < Z) acc += sq4(c, __ldg(v + i + 1));
+      if (y + 1 < Y) acc += sq4(c, __ldg(v + i + Z));
+      if (x + 1 < X) acc += sq4(c, __ldg(v + i + YZ));
+      if (++n == 32) {  // bound the fp32 run, then fold into fp64
+        acc_d += acc;
+        acc = 0.f;
+        n = 0;
+      }
     }
+    acc_d += acc;
   }
-  acc_d += acc;
   __shared__ double red[kTvThreads];
   __shared__ bool last;
   red[threadIdx.x] = acc_d;
@@ -59,18 +62,28 @@ __global__ void __launch_bounds__(kTvThreads) tv_sumsq_kernel(const float4* __re
     if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
+  const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned bid = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
   if (threadIdx.x == 0) {
-    partials[blockIdx.x] = red[0];
+    partials[bid] = red[0];
     __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1u;
+    last = atomicAdd(counter, 1u) == nblocks - 1u;
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
+  if (last) {
     __threadfence();
     double s = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) s += ((volatile double*)partials)[b];
-    out[0] = s;
-    *counter = 0u;
+    for (unsigned b = threadIdx.x; b < nblocks; b += blockDim.x) s += ((volatile double*)partials)[b];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kTvThreads / 2; w > 0; w >>= 1) {
+      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      out[0] = red[0];
+      *counter = 0u;
+    }
   }
 }
 
@@ -80,29 +93,25 @@ __global__ void tv_grad_kernel(const float4* __restrict__ v, int X, int Y, int Z
   const double q = sumsq[0];
   if (!(q > 0.0)) return;  // a constant grid: sqrt is not differentiable at 0
   const float c = (float)((double)weight / sqrt(q));
-  const int64_t G = (int64_t)X * Y * Z;
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  if (z >= Z) return;
+  const int y = blockIdx.y, x = blockIdx.z;
   const int64_t YZ = (int64_t)Y * Z;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < G;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(i % Z);
-    const int64_t ij = i / Z;
-    const int j = (int)(ij % Y);
-    const int x = (int)(ij / Y);
-    const float4 m = __ldg(v + i);
-    float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto add = [&](float4 nb) {
-      d.x += m.x - nb.x; d.y += m.y - nb.y; d.z += m.z - nb.z; d.w += m.w - nb.w;
-    };
-    if (k > 0) add(__ldg(v + i - 1));
-    if (k + 1 < Z) add(__ldg(v + i + 1));
-    if (j > 0) add(__ldg(v + i - Z));
-    if (j + 1 < Y) add(__ldg(v + i + Z));
-    if (x > 0) add(__ldg(v + i - YZ));
-    if (x + 1 < X) add(__ldg(v + i + YZ));
-    float4 g = grad[i];
-    g.x += c * d.x; g.y += c * d.y; g.z += c * d.z; g.w += c * d.w;
-    grad[i] = g;
-  }
+  const int64_t i = (int64_t)x * YZ + (int64_t)y * Z + z;
+  const float4 m = __ldg(v + i);
+  float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto add = [&](float4 nb) {
+    d.x += m.x - nb.x; d.y += m.y - nb.y; d.z += m.z - nb.z; d.w += m.w - nb.w;
+  };
+  if (z > 0) add(__ldg(v + i - 1));
+  if (z + 1 < Z) add(__ldg(v + i + 1));
+  if (y > 0) add(__ldg(v + i - Z));
+  if (y + 1 < Y) add(__ldg(v + i + Z));
+  if (x > 0) add(__ldg(v + i - YZ));
+  if (x + 1 < X) add(__ldg(v + i + YZ));
+  float4 g = grad[i];
+  g.x += c * d.x; g.y += c * d.y; g.z += c * d.z; g.w += c * d.w;
+  grad[i] = g;
 }
 
 struct AdamConst {
@@ -153,18 +162,20 @@ using namespace pgb;
 
 extern "C" {
 
-int64_t pgb_tv_workspace_bytes(void) { return (int64_t)sizeof(double) * kTvBlocks + 256; }
+// partial sums: one per block of the (z-blocks, Y, kTvXChunks) grid
+int64_t pgb_tv_workspace_bytes(void) { return (int64_t)sizeof(double) * kTvMaxBlocks + 256; }
 
 int pgb_tv_sumsq(const float* cells, const int32_t dims[3], double* sumsq_out, void* workspace,
                  pgb_stream_t stream) {
   if (!cells || !dims || !sumsq_out || !workspace) return PGB_ERR_ARG;
   if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return PGB_ERR_ARG;
   if (!al16(cells) || !al16(workspace)) return PGB_ERR_ALIGN;
-  const int64_t G = (int64_t)dims[0] * dims[1] * dims[2];
-  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((G + kTvThreads - 1) / kTvThreads, kTvBlocks));
-  tv_sumsq_kernel<<<blocks, kTvThreads, 0, stream>>>(
+  if (dims[1] > 65535) return PGB_ERR_UNSUPPORTED;
+  const dim3 grid((dims[2] + kTvThreads - 1) / kTvThreads, dims[1], std::min(dims[0], kTvXChunks));
+  if ((int64_t)grid.x * grid.y * grid.z > kTvMaxBlocks) return PGB_ERR_UNSUPPORTED;
+  tv_sumsq_kernel<<<grid, kTvThreads, 0, stream>>>(
       reinterpret_cast<const float4*>(cells), dims[0], dims[1], dims[2], (double*)workspace,
-      (unsigned*)((char*)workspace + sizeof(double) * kTvBlocks), sumsq_out);
+      (unsigned*)((char*)workspace + sizeof(double) * kTvMaxBlocks), sumsq_out);
   return after_launch();
 }
 
@@ -173,10 +184,10 @@ int pgb_tv_grad(const float* cells, const int32_t dims[3], const double* sumsq, 
   if (!cells || !dims || !sumsq || !grad_cells) return PGB_ERR_ARG;
   if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return PGB_ERR_ARG;
   if (!al16(cells) || !al16(grad_cells)) return PGB_ERR_ALIGN;
-  const int64_t G = (int64_t)dims[0] * dims[1] * dims[2];
-  tv_grad_kernel<<<stream_blocks(G), 256, 0, stream>>>(reinterpret_cast<const float4*>(cells), dims[0],
-                                                       dims[1], dims[2], sumsq, weight,
-                                                       reinterpret_cast<float4*>(grad_cells));
+  if (dims[0] > 65535 || dims[1] > 65535) return PGB_ERR_UNSUPPORTED;
+  const dim3 grid((dims[2] + 127) / 128, dims[1], dims[0]);
+  tv_grad_kernel<<<grid, 128, 0, stream>>>(reinterpret_cast<const float4*>(cells), dims[0], dims[1],
+                                           dims[2], sumsq, weight, reinterpret_cast<float4*>(grad_cells));
   return after_launch();
 }
 

@@ -37,6 +37,7 @@ struct GridP {
   Real ox, oy, oz;
   Real pd;
   int clip;
+  float alpha_floor;  // >0: clamped alpha below it reads as 0 (inference threshold)
 };
 
 template <typename Real>
@@ -229,6 +230,10 @@ __device__ __forceinline__ void sample_value(const GridP<Real>& g, Real nx, Real
         v[ch] = cv[ch];
       }
     }
+    if (g.alpha_floor > 0.0f && v[3] < (Real)g.alpha_floor) {
+      v[3] = Real(0);
+      bits &= ~8u;
+    }
   } else {
     Corners<Real> q;
     if (!trilinear_corners(g, nx, ny, nz, q)) return;
@@ -251,6 +256,10 @@ __device__ __forceinline__ void sample_value(const GridP<Real>& g, Real nx, Real
           bits |= 1u << (4 * corner + ch);
         }
       }
+      if (g.alpha_floor > 0.0f && cv[corner][3] < (Real)g.alpha_floor) {
+        cv[corner][3] = Real(0);
+        bits &= ~(8u << (4 * corner));
+      }
     }
     // blend x, then y, then z, as src/grid_functions.py:34-42
     const Real wx = q.w[0], wy = q.w[1], wz = q.w[2];
@@ -268,10 +277,19 @@ __device__ __forceinline__ void sample_value(const GridP<Real>& g, Real nx, Real
   }
 }
 
+#ifndef PGB_SCATTER_INLINE
+#define PGB_SCATTER_INLINE 1
+#endif
+#if PGB_SCATTER_INLINE
+#define PGB_SCATTER_ATTR __device__ __forceinline__
+#else
+#define PGB_SCATTER_ATTR __device__ __noinline__
+#endif
+
 // Scatter dL/dvalue of one sample into the dense gradient (the autograd replay of the
 // blend, the clamp mask and index_put accumulate).
 template <typename Real, int MODE>
-__device__ __forceinline__ void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, Real ny,
+PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, Real ny,
                                                Real nz, const Real dv[4], uint32_t bits) {
   if (bits == 0u) return;
   if (MODE == PGB_NEAREST) {

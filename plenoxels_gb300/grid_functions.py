@@ -7,10 +7,12 @@ be CUDA tensors (there is no CPU path). Functions that the reference differentia
 scatter kernel.
 
 Out of scope (not on the render path): voxel_average, get_receptive_field_voxels,
-average_pool3d_grid, gaussian/filled-circle kernels and convolve_grid_to_remove_noise.
+gaussian/filled-circle kernels and convolve_grid_to_remove_noise. average_pool3d_grid (the
+coarse-to-fine pooling the training loop feeds into the path) is provided.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 
 import numpy as np
@@ -232,3 +234,49 @@ def trilinear_interpolation(normalized_samples_for_indecies, selected_points, gr
     if selected_points.dtype != torch.int64 or tuple(selected_points.shape[1:]) != (8, 3):
         raise ValueError("trilinear_interpolation: selected_points must be int64 [N,8,3]")
     return _Trilinear.apply(n, selected_points.contiguous(), grid_cells.contiguous(), bool(clip))
+
+
+def pool_shape(shape, window, stride):
+    """(out_dims, scratch bytes) of average_pool3d_grid on a [X,Y,Z,4] grid."""
+    od = (ctypes.c_int32 * 3)()
+    nbytes = ctypes.c_int64(0)
+    check(_lib.load().pgb_avg_pool3d_shape(_lib.dims3(shape), int(window), int(stride), od,
+                                           ctypes.byref(nbytes)), "average_pool3d_grid")
+    return (od[0], od[1], od[2]), int(nbytes.value)
+
+
+class _AvgPool(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, grid, window, stride):
+        od, nbytes = pool_shape(grid.shape, window, stride)
+        scratch = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=grid.device)
+        out = torch.empty(*od, 4, dtype=torch.float32, device=grid.device)
+        check(_lib.load().pgb_avg_pool3d_fwd(ptr(grid), _lib.dims3(grid.shape), window, stride,
+                                             ptr(scratch), ptr(out), stream_of(grid)),
+              "average_pool3d_grid")
+        ctx.shape, ctx.window, ctx.stride = tuple(grid.shape), window, stride
+        return out
+
+    @staticmethod
+    def backward(ctx, d_out):
+        _, nbytes = pool_shape(ctx.shape, ctx.window, ctx.stride)
+        d_out = d_out.to(torch.float32).contiguous()
+        scratch = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=d_out.device)
+        d_in = torch.empty(ctx.shape, dtype=torch.float32, device=d_out.device)
+        check(_lib.load().pgb_avg_pool3d_bwd(ptr(d_out), _lib.dims3(ctx.shape), ctx.window,
+                                             ctx.stride, ptr(scratch), ptr(d_in),
+                                             stream_of(d_out)), "average_pool3d_grid backward")
+        return d_in, None, None
+
+
+def average_pool3d_grid(tensor, receptive_field_size=3, stride=None):
+    """src/grid_functions.py:173-181: [X,Y,Z,4] -> [Xo,Yo,Zo,4] average over cubic windows
+    of receptive_field_size cells with the given stride (default: the window), no
+    padding. Returns a contiguous tensor (the reference returns a permuted view of the
+    same values). Differentiable."""
+    require_cuda(tensor)
+    if tensor.dim() != 4 or tensor.shape[-1] != 4 or tensor.dtype != torch.float32:
+        raise ValueError("average_pool3d_grid takes a float32 [X,Y,Z,4] grid")
+    r = int(receptive_field_size)
+    s = r if stride is None else int(stride)
+    return _AvgPool.apply(tensor.contiguous(), r, s)

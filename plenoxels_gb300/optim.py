@@ -33,14 +33,16 @@ class FusedAdam:
         self._tv_ws = torch.zeros(lib.pgb_tv_workspace_bytes(), dtype=torch.uint8, device=grid.device)
         self.tv_sumsq = torch.zeros((), dtype=torch.float64, device=grid.device)
 
-    def add_tv(self, grad, weight):
+    def add_tv(self, grad, weight, grid=None):
         """Adds the gradient of weight * tv_loss(grid) (scripts/train.py:163-165) to grad;
-        returns the term's value as a device scalar."""
+        returns the term's value as a device scalar. grid defaults to the optimised grid
+        (the pooled grid while progressive growing runs)."""
+        grid = self.grid if grid is None else grid
         lib = _lib.load()
-        s = torch.cuda.current_stream(self.grid.device).cuda_stream
-        dims = _lib.dims3(self.grid.shape)
-        check(lib.pgb_tv_sumsq(ptr(self.grid), dims, ptr(self.tv_sumsq), ptr(self._tv_ws), s), "tv loss")
-        check(lib.pgb_tv_grad(ptr(self.grid), dims, ptr(self.tv_sumsq), float(weight), ptr(grad), s),
+        s = torch.cuda.current_stream(grid.device).cuda_stream
+        dims = _lib.dims3(grid.shape)
+        check(lib.pgb_tv_sumsq(ptr(grid), dims, ptr(self.tv_sumsq), ptr(self._tv_ws), s), "tv loss")
+        check(lib.pgb_tv_grad(ptr(grid), dims, ptr(self.tv_sumsq), float(weight), ptr(grad), s),
               "tv loss")
         return float(weight) * self.tv_sumsq.sqrt()
 
