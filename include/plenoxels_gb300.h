@@ -319,6 +319,25 @@ int pgb_composite_bwd(const void* samples, int32_t dtype, int64_t num_rays, int3
  * image_out[a][b] is ray b * res + a. */
 int pgb_rgba_to_image(const float* rgba, int32_t res, uint8_t* image_out, pgb_stream_t stream);
 
+/* ---- previews and clean-up (src/visualization.py:157-232, src/grid_functions.py:260-280) ---- */
+
+/* Width xs of the splat preview of a camera (host transform, row-major 4x4) of height
+ * size_y: int(size_y * |x axis| / |y axis|), fp32 as the reference computes it. */
+int pgb_splat_size(const float* transform, int32_t size_y, int32_t* width_out);
+/* Point-splat preview (visulize_3d_in_2d_fast): every cell of a contiguous fp32
+ * [X,Y,Z,4] grid with alpha > alpha_min projects to a pixel of an [xs, size_y] image; the
+ * nearest such cell paints its RGB, other pixels are white. transform is a HOST pointer.
+ * keys_scratch holds xs * size_y uint64; image_out is [xs, size_y, 3] fp32. */
+int pgb_splat_preview(const float* cells, const int32_t dims[3], float points_distance,
+                      const float* transform, float camera_angle_x, int32_t size_y, float alpha_min,
+                      unsigned long long* keys_scratch, float* image_out, pgb_stream_t stream);
+/* convolve_grid_to_remove_noise on a contiguous fp32 [X,Y,Z,4] grid, in place: `repeats`
+ * times, every cell whose summed neighbour alpha over the filled ball (kernel_size^3,
+ * offsets with distance <= radius, centre excluded, zero padding) is below threshold is
+ * cleared. kernel_size odd and <= 7; sums_scratch holds X*Y*Z floats. */
+int pgb_remove_noise(float* cells, const int32_t dims[3], int32_t kernel_size, double radius,
+                     float threshold, int32_t repeats, float* sums_scratch, pgb_stream_t stream);
+
 /* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel. */
 int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream);
 

@@ -266,3 +266,53 @@ def average_pool3d_grid(tensor, receptive_field_size=3, stride=None):
     x = tensor.permute(3, 0, 1, 2).unsqueeze(0)
     r = (receptive_field_size,) * 3
     return torch.nn.functional.avg_pool3d(x, r, stride=stride).squeeze(0).permute(1, 2, 3, 0)
+
+
+def remove_noise(grid_cells, kernel_size=3, radius=1.0, threshold=2, repeats=20):
+    """src/grid_functions.py:260-280: filled-ball conv3d of alpha, clear cells below the
+    threshold, repeated (in place)."""
+    k = np.linspace(-(kernel_size // 2), kernel_size // 2, kernel_size)
+    x, y, z = np.meshgrid(k, k, k)
+    d = np.sqrt(x * x + y * y + z * z)
+    w = np.where(d <= radius, 1, 0)
+    w[kernel_size // 2, kernel_size // 2, kernel_size // 2] = 0
+    w = torch.from_numpy(w).float().unsqueeze(0).unsqueeze(0)
+    w = w / w.max()
+    for _ in range(repeats):
+        out = torch.nn.functional.conv3d(grid_cells[..., -1].unsqueeze(0), w, padding="same")[0]
+        grid_cells[out < threshold] = 0
+    return grid_cells
+
+
+def splat_preview(grid, points_distance, transform_matrix, camera_angle_x, size_y):
+    """src/visualization.py:157-232 (visulize_3d_in_2d_fast), same ops; returns the image,
+    the pixel of every drawn point and its distance."""
+    rot = transform_matrix[:3, :3]
+    pos = transform_matrix[:3, 3]
+    yz = transform_matrix[:3, 0]
+    xz = transform_matrix[:3, 1]
+    aspect = yz.norm(dim=0) / xz.norm(dim=0)
+    cond = grid[..., 3] > 0.1
+    pts = np.argwhere(cond)
+    colors = grid[cond]
+    half = (torch.tensor(grid.shape[:3]) / 2).unsqueeze(1).ceil()
+    pts = ((pts - half) + 1)
+    pts = (pts * points_distance).T
+    ctp = pts - pos
+    a = torch.matmul(ctp, yz)
+    b = torch.matmul(ctp, xz)
+    nm = ctp.norm(dim=1) * yz.norm()
+    ax, ay = a / nm, b / nm
+    xn = 0.5 + ay / -camera_angle_x
+    yn = 0.5 + ax / (camera_angle_x / aspect)
+    ok = (xn < 1.0).logical_and(xn >= 0.0).logical_and(yn < 1.0).logical_and(yn >= 0.0)
+    xn, yn, colors, ctp = xn[ok], yn[ok], colors[ok], ctp[ok]
+    ys = size_y
+    xs = int(ys * aspect)
+    xx = (xs * xn).round().clamp(min=0, max=xs - 1).type(torch.long)
+    yy = (ys * yn).round().clamp(min=0, max=ys - 1).type(torch.long)
+    dist = ctp.norm(dim=1)
+    order = torch.argsort(-dist)
+    img = np.ones([xs, ys, 3])
+    img[xx[order], yy[order]] = colors[order][:, :3]
+    return img, xx, yy, dist

@@ -23,6 +23,8 @@ LIB_PATH = os.path.join(PKG_DIR, "libplenoxels_gb300.so")
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + [
     "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+    # host-side fp32 arithmetic (splat camera constants) must round op by op on Arm too
+    "-Xcompiler", "-ffp-contract=off",
     # index arithmetic must round op by op: never let nvcc contract or approximate
     "-fmad=true", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
     f"-I{INCLUDE}", f"-I{CSRC}",

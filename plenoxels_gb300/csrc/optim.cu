@@ -25,8 +25,9 @@ __device__ __forceinline__ float sq4(float4 a, float4 b) {
   return x * x + y * y + z * z + w * w;
 }
 
-// Block (bz, y, xc) covers z in [bz*T, bz*T + T) of row y for the x values x = xc, xc + XC,
-// ...: no integer division per cell, coalesced along z.
+// Block (bz, y, xc) covers z in [bz*T, bz*T + T) of row y and the run of consecutive x
+// values xc*XL .. xc*XL + XL - 1, so the x-neighbours come from the previous and next
+// iteration's registers; no integer division per cell, coalesced along z.
 constexpr int kTvXChunks = 8;
 
 __global__ void __launch_bounds__(kTvThreads) tv_sumsq_kernel(const float4* __restrict__ v, int X, int Y,
@@ -36,20 +37,25 @@ __global__ void __launch_bounds__(kTvThreads) tv_sumsq_kernel(const float4* __re
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   const int64_t YZ = (int64_t)Y * Z;
+  const int XL = (X + gridDim.z - 1) / gridDim.z;
+  const int x0 = blockIdx.z * XL, x1 = min(X, x0 + XL);
   double acc_d = 0.0;
-  if (z < Z) {
+  if (z < Z && x0 < x1) {
     float acc = 0.f;
-    int n = 0;
-    for (int x = blockIdx.z; x < X; x += gridDim.z) {
-      const int64_t i = (int64_t)x * YZ + (int64_t)y * Z + z;
-      const float4 c = __ldg(v + i);
+    int64_t i = (int64_t)x0 * YZ + (int64_t)y * Z + z;
+    float4 c = __ldg(v + i);
+    for (int x = x0; x < x1; ++x, i += YZ) {
       if (z + 1 < Z) acc += sq4(c, __ldg(v + i + 1));
       if (y + 1 < Y) acc += sq4(c, __ldg(v + i + Z));
-      if (x + 1 < X) acc += sq4(c, __ldg(v + i + YZ));
-      if (++n == 32) {  // bound the fp32 run, then fold into fp64
+      float4 nx = c;
+      if (x + 1 < X) {
+        nx = __ldg(v + i + YZ);
+        acc += sq4(c, nx);
+      }
+      c = nx;
+      if (((x - x0) & 31) == 31) {  // bound the fp32 run, then fold into fp64
         acc_d += acc;
         acc = 0.f;
-        n = 0;
       }
     }
     acc_d += acc;
@@ -87,31 +93,39 @@ __global__ void __launch_bounds__(kTvThreads) tv_sumsq_kernel(const float4* __re
   }
 }
 
-__global__ void tv_grad_kernel(const float4* __restrict__ v, int X, int Y, int Z,
-                               const double* __restrict__ sumsq, float weight,
-                               float4* __restrict__ grad) {
+__global__ void __launch_bounds__(kTvThreads) tv_grad_kernel(const float4* __restrict__ v, int X, int Y,
+                                                             int Z, const double* __restrict__ sumsq,
+                                                             float weight, float4* __restrict__ grad) {
   const double q = sumsq[0];
   if (!(q > 0.0)) return;  // a constant grid: sqrt is not differentiable at 0
   const float c = (float)((double)weight / sqrt(q));
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
-  if (z >= Z) return;
-  const int y = blockIdx.y, x = blockIdx.z;
+  const int y = blockIdx.y;
+  const int XL = (X + gridDim.z - 1) / gridDim.z;
+  const int x0 = blockIdx.z * XL, x1 = min(X, x0 + XL);
+  if (z >= Z || x0 >= x1) return;
   const int64_t YZ = (int64_t)Y * Z;
-  const int64_t i = (int64_t)x * YZ + (int64_t)y * Z + z;
-  const float4 m = __ldg(v + i);
-  float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
-  auto add = [&](float4 nb) {
-    d.x += m.x - nb.x; d.y += m.y - nb.y; d.z += m.z - nb.z; d.w += m.w - nb.w;
-  };
-  if (z > 0) add(__ldg(v + i - 1));
-  if (z + 1 < Z) add(__ldg(v + i + 1));
-  if (y > 0) add(__ldg(v + i - Z));
-  if (y + 1 < Y) add(__ldg(v + i + Z));
-  if (x > 0) add(__ldg(v + i - YZ));
-  if (x + 1 < X) add(__ldg(v + i + YZ));
-  float4 g = grad[i];
-  g.x += c * d.x; g.y += c * d.y; g.z += c * d.z; g.w += c * d.w;
-  grad[i] = g;
+  int64_t i = (int64_t)x0 * YZ + (int64_t)y * Z + z;
+  float4 prev = x0 > 0 ? __ldg(v + i - YZ) : make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 m = __ldg(v + i);
+  for (int x = x0; x < x1; ++x, i += YZ) {
+    const float4 next = x + 1 < X ? __ldg(v + i + YZ) : m;
+    float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto add = [&](float4 nb) {
+      d.x += m.x - nb.x; d.y += m.y - nb.y; d.z += m.z - nb.z; d.w += m.w - nb.w;
+    };
+    if (z > 0) add(__ldg(v + i - 1));
+    if (z + 1 < Z) add(__ldg(v + i + 1));
+    if (y > 0) add(__ldg(v + i - Z));
+    if (y + 1 < Y) add(__ldg(v + i + Z));
+    if (x > 0) add(prev);
+    if (x + 1 < X) add(next);
+    float4 g = grad[i];
+    g.x += c * d.x; g.y += c * d.y; g.z += c * d.z; g.w += c * d.w;
+    grad[i] = g;
+    prev = m;
+    m = next;
+  }
 }
 
 struct AdamConst {
@@ -184,10 +198,10 @@ int pgb_tv_grad(const float* cells, const int32_t dims[3], const double* sumsq, 
   if (!cells || !dims || !sumsq || !grad_cells) return PGB_ERR_ARG;
   if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return PGB_ERR_ARG;
   if (!al16(cells) || !al16(grad_cells)) return PGB_ERR_ALIGN;
-  if (dims[0] > 65535 || dims[1] > 65535) return PGB_ERR_UNSUPPORTED;
-  const dim3 grid((dims[2] + 127) / 128, dims[1], dims[0]);
-  tv_grad_kernel<<<grid, 128, 0, stream>>>(reinterpret_cast<const float4*>(cells), dims[0], dims[1],
-                                           dims[2], sumsq, weight, reinterpret_cast<float4*>(grad_cells));
+  if (dims[1] > 65535) return PGB_ERR_UNSUPPORTED;
+  const dim3 grid((dims[2] + kTvThreads - 1) / kTvThreads, dims[1], std::min(dims[0], kTvXChunks));
+  tv_grad_kernel<<<grid, kTvThreads, 0, stream>>>(reinterpret_cast<const float4*>(cells), dims[0], dims[1],
+                                                  dims[2], sumsq, weight, reinterpret_cast<float4*>(grad_cells));
   return after_launch();
 }
 

@@ -6,9 +6,9 @@ be CUDA tensors (there is no CPU path). Functions that the reference differentia
 (lookups of the grid) are ``torch.autograd.Function``s whose backward is a hand-written
 scatter kernel.
 
-Out of scope (not on the render path): voxel_average, get_receptive_field_voxels,
-gaussian/filled-circle kernels and convolve_grid_to_remove_noise. average_pool3d_grid (the
-coarse-to-fine pooling the training loop feeds into the path) is provided.
+Also provided: average_pool3d_grid (the coarse-to-fine pooling the training loop feeds
+into the path) and convolve_grid_to_remove_noise (the stray-voxel clean-up applied before
+viewing). Out of scope: voxel_average, get_receptive_field_voxels and the kernel helpers.
 """
 from __future__ import annotations
 
@@ -280,3 +280,20 @@ def average_pool3d_grid(tensor, receptive_field_size=3, stride=None):
     r = int(receptive_field_size)
     s = r if stride is None else int(stride)
     return _AvgPool.apply(tensor.contiguous(), r, s)
+
+
+@torch.no_grad()
+def convolve_grid_to_remove_noise(grid_cells, kernel_size=3, radius=1.0, threshold=2, repeats=20):
+    """src/grid_functions.py:270-280: `repeats` times, cells whose summed neighbour alpha
+    over the filled ball (distance <= radius, centre excluded, zero padding) is below
+    threshold are cleared, in place; returns grid_cells."""
+    require_cuda(grid_cells)
+    if grid_cells.dim() != 4 or grid_cells.shape[-1] != 4 or grid_cells.dtype != torch.float32:
+        raise ValueError("convolve_grid_to_remove_noise takes a float32 [X,Y,Z,4] grid")
+    if not grid_cells.is_contiguous():
+        raise ValueError("convolve_grid_to_remove_noise works in place on a contiguous grid")
+    sums = torch.empty(grid_cells.shape[:3], dtype=torch.float32, device=grid_cells.device)
+    check(_lib.load().pgb_remove_noise(ptr(grid_cells), _lib.dims3(grid_cells.shape), int(kernel_size),
+                                       float(radius), float(threshold), int(repeats), ptr(sums),
+                                       stream_of(grid_cells)), "convolve_grid_to_remove_noise")
+    return grid_cells
