@@ -75,6 +75,8 @@ typedef struct {
   int32_t stratified;       /* 1: t_k = delta_step * (k - j_k), j_k in [0,1) from the hash */
   uint64_t seed;            /* stratification seed */
   float term_threshold;     /* >0: stop a ray once its transmittance falls below this */
+  int32_t use_background;   /* 1: output rgb += (1 - alpha) * background (alpha unchanged) */
+  float background[3];      /* e.g. 1,1,1 for a white background; the reference has none */
 } pgb_rays;
 
 /* ---- fused render path (scripts/train.py:142-156 composed with src/ray_sampling.py,

@@ -187,9 +187,10 @@ def composite(samples):
 
 # ----------------------------------------------------------------------- full path
 def render(grid, origins, dirs, num_samples: int, delta_step: float, gmin, points_distance: float,
-           mode: str = "trilinear", clip: bool = True, jitter=None):
+           mode: str = "trilinear", clip: bool = True, jitter=None, background=None):
     """rgba [R,4] of rays through the grid: scripts/train.py:142-153 with the lookup
-    chosen by mode. Differentiable in grid through torch autograd."""
+    chosen by mode; background (harness term, e.g. white) composites rgb over it.
+    Differentiable in grid through torch autograd."""
     R = origins.shape[0]
     pts = sample_positions(origins, dirs, num_samples, delta_step, jitter)
     n = normalize(pts, gmin, points_distance)
@@ -201,14 +202,18 @@ def render(grid, origins, dirs, num_samples: int, delta_step: float, gmin, point
     else:
         raise ValueError(mode)
     vals = vals * mask.unsqueeze(-1)
-    return composite(vals.reshape(1, R, num_samples, 4)).reshape(R, 4)
+    px = composite(vals.reshape(1, R, num_samples, 4)).reshape(R, 4)
+    if background is not None:
+        bg = torch.as_tensor(background, dtype=px.dtype)
+        px = torch.cat([px[:, :3] + (1 - px[:, 3:]) * bg, px[:, 3:]], 1)
+    return px
 
 
 def train_loss(grid, origins, dirs, target, num_samples, delta_step, gmin, points_distance,
-               mode="trilinear", clip=True, jitter=None):
+               mode="trilinear", clip=True, jitter=None, background=None):
     """mse_loss(render, target), scripts/train.py:156."""
     px = render(grid, origins, dirs, num_samples, delta_step, gmin, points_distance, mode, clip,
-                jitter)
+                jitter, background)
     return torch.nn.functional.mse_loss(px, target)
 
 

@@ -58,6 +58,8 @@ class PgbRays(Structure):
         ("stratified", c_int32),
         ("seed", c_uint64),
         ("term_threshold", c_float),
+        ("use_background", c_int32),
+        ("background", c_float * 3),
     ]
 
 

@@ -115,6 +115,8 @@ RenderArgs<Real> render_args(const pgb_grid* g, const pgb_rays* r) {
   a.stratified = r->stratified ? 1 : 0;
   a.strat_seed = r->seed;
   a.term_thr = r->term_threshold;
+  a.use_bg = r->use_background ? 1 : 0;
+  for (int c = 0; c < 3; ++c) a.bg[c] = r->background[c];
   return a;
 }
 

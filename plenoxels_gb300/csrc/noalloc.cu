@@ -84,6 +84,8 @@ int launch_noalloc(const pgb_grid* g, const pgb_rays* r, const void* target, dou
   a.stratified = r->stratified ? 1 : 0;
   a.strat_seed = r->seed;
   a.term_thr = r->term_threshold;
+  a.use_bg = r->use_background ? 1 : 0;
+  for (int c = 0; c < 3; ++c) a.bg[c] = r->background[c];
   a.rgba_out = (Real*)rgba_out;
   a.target = (const Real*)target;
   a.grad = (Real*)grad_cells;

@@ -60,6 +60,8 @@ struct RenderArgs {
   int stratified;
   uint64_t strat_seed;
   float term_thr;
+  int use_bg;      // rgb += (1 - A) * bg after compositing
+  float bg[3];
   // outputs / adjoint inputs
   Real* rgba_out;
   const Real* d_rgba;
@@ -364,6 +366,23 @@ struct CoordStage {
   }
 };
 
+#ifndef PGB_RENDER_GATHER_INLINE
+#define PGB_RENDER_GATHER_INLINE 1
+#endif
+#if PGB_RENDER_GATHER_INLINE
+#define PGB_RENDER_GATHER_ATTR __device__ __forceinline__
+#else
+#define PGB_RENDER_GATHER_ATTR __device__ __noinline__
+#endif
+
+// One sample of a ray: coordinates and value (zero outside the grid).
+template <typename Real, typename Store, int MODE>
+PGB_RENDER_GATHER_ATTR void render_sample(const RenderArgs<Real>& a, const Ray<Real>& ray, int s,
+                                          Real v[4], uint32_t& bits, Real& nx, Real& ny, Real& nz) {
+  sample_coords(a, ray, s, nx, ny, nz);
+  sample_value<Real, Store, MODE>(a.g, nx, ny, nz, v, bits);
+}
+
 // Gathers chunk `c` (K slots) of a ray into registers (and its coordinates into the
 // stage when the adjoint follows).
 template <typename Real, typename Store, int MODE, int K, bool ADJ>
@@ -381,8 +400,7 @@ __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ra
     bits[k] = 0u;
     if (s < a.S) {
       Real nx, ny, nz;
-      sample_coords(a, ray, s, nx, ny, nz);
-      sample_value<Real, Store, MODE>(a.g, nx, ny, nz, v[k], bits[k]);
+      render_sample<Real, Store, MODE>(a, ray, s, v[k], bits[k], nx, ny, nz);
       if (ADJ && PGB_COORDS_IN_SMEM) cs.put(k, lane, nx, ny, nz);
     }
   }
@@ -475,6 +493,10 @@ render_kernel(const RenderArgs<Real> a) {
     Real px[4];
 #pragma unroll
     for (int ch = 0; ch < 4; ++ch) px[ch] = warp_sum(acc[ch]);
+    if (a.use_bg) {
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) px[ch] += (Real(1) - px[3]) * (Real)a.bg[ch];
+    }
 
     if (PHASE == kForward) {
       if (lane < 4) a.rgba_out[4 * r + lane] = pick4(px, lane);
@@ -496,6 +518,8 @@ render_kernel(const RenderArgs<Real> a) {
       if (lane == 0) loss_lane += sq;
       if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = pick4(px, lane);
     }
+    if (a.use_bg)  // d(rgb + (1 - A) bg)/dA = -bg
+      gpx[3] -= gpx[0] * (Real)a.bg[0] + gpx[1] * (Real)a.bg[1] + gpx[2] * (Real)a.bg[2];
 
     // reverse pass over the chunks that were composited
     Real Snext_carry = Real(0);  // S at the first sample after the current slot

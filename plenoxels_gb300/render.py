@@ -27,7 +27,7 @@ def _mode(mode) -> int:
 
 
 def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, seed, term_threshold,
-               cameras=None) -> PgbRays:
+               cameras=None, background=None) -> PgbRays:
     r = PgbRays()
     r.origins = ptr(origins)
     r.dirs = ptr(dirs)
@@ -38,6 +38,9 @@ def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, see
     r.stratified = 1 if stratified else 0
     r.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
     r.term_threshold = float(term_threshold)
+    if background is not None:
+        r.use_background = 1
+        r.background[:] = [float(v) for v in background]
     return r
 
 
@@ -60,7 +63,8 @@ class _RenderRays(torch.autograd.Function):
         rgba = torch.empty(R, 4, dtype=_lib.real_dtype(grid.dtype), device=grid.device)
         gdesc = _lib.make_grid(grid, cfg["origin"], cfg["points_distance"], cfg["mode"], cfg["clip"])
         rdesc = _rays_desc(origins, dirs, R, cfg["num_samples"], cfg["delta_step"],
-                           cfg["stratified"], cfg["seed"], cfg["term_threshold"])
+                           cfg["stratified"], cfg["seed"], cfg["term_threshold"],
+                           background=cfg["background"])
         check(lib.pgb_render_fwd(gdesc, rdesc, ptr(rgba), stream_of(grid)), "render_rays")
         ctx.save_for_backward(grid, origins, dirs)
         ctx.cfg = cfg
@@ -77,18 +81,21 @@ class _RenderRays(torch.autograd.Function):
         d_rgba = d_rgba.to(grad.dtype).contiguous()
         gdesc = _lib.make_grid(grid, cfg["origin"], cfg["points_distance"], cfg["mode"], cfg["clip"])
         rdesc = _rays_desc(origins, dirs, origins.shape[0], cfg["num_samples"], cfg["delta_step"],
-                           cfg["stratified"], cfg["seed"], cfg["term_threshold"])
+                           cfg["stratified"], cfg["seed"], cfg["term_threshold"],
+                           background=cfg["background"])
         check(lib.pgb_render_bwd(gdesc, rdesc, ptr(d_rgba), ptr(grad), s), "render_rays backward")
         return grad, None, None, None
 
 
 def render_rays(grid, origins, dirs, delta_step, num_samples, points_distance, grid_min=None,
-                mode="trilinear", clip=True, stratified=False, seed=0, term_threshold=0.0):
+                mode="trilinear", clip=True, stratified=False, seed=0, term_threshold=0.0,
+                background=None):
     """Premultiplied RGBA [R,4] of rays through a dense [X,Y,Z,4] grid.
 
     Samples sit at origins + dirs * (delta_step * k), k = 1..num_samples (minus a
     per-sample jitter in [0,1) when stratified); grid_min is the world position of cell
-    (0,0,0) (default: generate_grid's layout, grid_origin()). Differentiable in grid."""
+    (0,0,0) (default: generate_grid's layout, grid_origin()). background (3 values, e.g. white)
+    composites rgb over it: rgb + (1 - alpha) * background. Differentiable in grid."""
     require_cuda(grid, origins, dirs)
     _check_rays(grid, origins, dirs)
     if grid_min is None:
@@ -96,7 +103,8 @@ def render_rays(grid, origins, dirs, delta_step, num_samples, points_distance, g
     cfg = dict(origin=tuple(float(x) for x in grid_min), points_distance=float(points_distance),
                mode=_mode(mode), clip=bool(clip), num_samples=int(num_samples),
                delta_step=float(delta_step), stratified=bool(stratified), seed=int(seed),
-               term_threshold=float(term_threshold))
+               term_threshold=float(term_threshold),
+               background=None if background is None else tuple(float(v) for v in background))
     return _RenderRays.apply(grid.contiguous(), origins.contiguous(), dirs.contiguous(), cfg)
 
 
@@ -180,7 +188,7 @@ class FusedTrainStep:
 
     def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
                  grid_min=None, clip=True, stratified=False, seed=0, term_threshold=0.0,
-                 loss_weight=1.0, overlap_zero=False, beta=0.0, beta_eps=1e-4):
+                 loss_weight=1.0, overlap_zero=False, beta=0.0, beta_eps=1e-4, background=None):
         require_cuda(grid)
         if grid.dim() != 4 or grid.shape[-1] != 4 or not grid.is_contiguous():
             raise ValueError("grid must be a contiguous [X,Y,Z,4] tensor")
@@ -199,6 +207,7 @@ class FusedTrainStep:
         self.loss_weight = float(loss_weight)
         self.beta = float(beta)
         self.beta_eps = float(beta_eps)
+        self.background = None if background is None else tuple(float(v) for v in background)
         lib = _lib.load()
         dev = grid.device
         self.workspace = torch.zeros(lib.pgb_train_workspace_bytes(), dtype=torch.uint8, device=dev)
@@ -283,7 +292,7 @@ class FusedTrainStep:
         if target.shape != (origins.shape[0], 4) or target.dtype != self.real:
             raise ValueError(f"target must be [R,4] {self.real}")
         rdesc = _rays_desc(origins, dirs, origins.shape[0], self.num_samples, self.delta_step,
-                           self.stratified, self.seed, self.term_threshold)
+                           self.stratified, self.seed, self.term_threshold, background=self.background)
         return self._launch(rdesc, target.contiguous(), rgba_out, zero_grad)
 
     def step_cameras(self, transforms, images, camera_angle_x, num_rays, ray_seed, near=0.0,
@@ -294,5 +303,5 @@ class FusedTrainStep:
         cams = _camera_desc(transforms, images, camera_angle_x, ray_seed, near)
         self._cams = cams  # keep alive for the call
         rdesc = _rays_desc(None, None, num_rays, self.num_samples, self.delta_step, self.stratified,
-                           self.seed, self.term_threshold, cameras=cams)
+                           self.seed, self.term_threshold, cameras=cams, background=self.background)
         return self._launch(rdesc, None, rgba_out, zero_grad)
