@@ -42,6 +42,7 @@ WORKLOAD = dict(workload="train step, 256^3 fp32 grid, 100 cams 800x800, 8192 ra
                          "stratified samples, trilinear", grid=256, cameras=100, image=800,
                 rays=8192, samples=256, mode="trilinear", near=2.0, far=6.0, blobs=16,
                 camera_angle_x=0.691)
+NCU_TRAFFIC_BYTES = 446_778_112 + 35_163_904  # DRAM read + write, one launch
 METRIC = "train rays/sec (fwd+bwd)"
 
 
@@ -467,13 +468,17 @@ def main():
             torch.distributed.destroy_process_group()
         return
 
-    # roofline of the fused kernel: algorithmic bytes per launch / measured duration
+    # roofline of the fused kernel: algorithmic bytes per launch / measured duration.
+    # traffic: dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on
+    # this workload under ncu (profiles/render_train_trilinear_256cube_ncu.md)
     U, inb_frac = unique_cells(pg, grid, T, imgs, W, 1000 * rank + args.warmup, delta, pd)
     alg_bytes = U * 16 + U * 16 + R * 60
     peak, peak_kind = _peaks()
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "kernel": "render_kernel<trilinear,train>",
+                "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
+                "traffic_unit": "bytes per launch (ncu capture of this workload)",
+                "kernel": "render_kernel<trilinear,train>",
                 "kernel_ms": kern_ms, "unique_cells": U, "algorithmic_bytes": alg_bytes,
                 "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "issued_gather_bytes": int(R * S * inb_frac * 8 * 16),
