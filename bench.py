@@ -217,6 +217,42 @@ def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup):
             "and gradients, cells stored in this type"}
 
 
+def random_access_ceiling(pg, dev, reads=1 << 24, reps=5):
+    """The GPU's rate for independent random 32 B sectors out of a 256 MiB buffer (16 B
+    loads, and float4 atomic adds), each launch after a 256 MiB write that evicts L2:
+    the ceiling for gathers and scatters with no reuse, as the render kernels do."""
+    from plenoxels_gb300 import _lib
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    nbytes = 256 << 20
+    table = torch.zeros(nbytes // 4, device=dev)
+    flush = torch.empty(nbytes // 4, device=dev)
+    sink = torch.zeros(1, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = {}
+    for kind in ("reads", "atomics"):
+        n = reads if kind == "reads" else reads // 4
+        ms = []
+        for rep in range(reps + 1):
+            _lib.check(lib.pgb_fill_zero(flush.data_ptr(), nbytes, stream))
+            e0.record()
+            if kind == "reads":
+                st = lib.pgb_probe_random_reads(table.data_ptr(), nbytes, n, 17 + rep, sink.data_ptr(), stream)
+            else:
+                st = lib.pgb_probe_random_atomics(table.data_ptr(), nbytes, n, 17 + rep, stream)
+            e1.record()
+            _lib.check(st)
+            torch.cuda.synchronize(dev)
+            if rep:
+                ms.append(e0.elapsed_time(e1))
+        best[kind] = n / (min(ms) / 1e3) / 1e9
+    del table, flush
+    return {"read_gsectors_per_s": best["reads"], "read_sector_gbs": best["reads"] * 32,
+            "atomic_gupdates_per_s": best["atomics"],
+            "probe": "2^24 random 16 B loads / 2^22 random float4 atomic adds over 256 MiB, "
+                     "L2 evicted before each launch, best of 5"}
+
+
 def batched_leg(pg, dev, steps=30, seed=11, num_scenes=64):
     """Batched form: 64 scenes (sides from {32,64,128,256}), 5 % occupied cells, BF16
     cells, rays per scene log-uniform in [1k, 64k], 512 samples per ray, early
@@ -492,6 +528,13 @@ def main():
                            parallelism=f"dp{world}" if world > 1 else "single"),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "clocks": clk.summary()}
+    rnd = random_access_ceiling(pg, dev)
+    roofline["random_access_ceiling"] = rnd
+    # DRAM sector traffic of one launch (ncu) at the measured kernel time, against the
+    # random-sector read rate: above 1 means the kernel's sectors have more locality
+    # (z-adjacent corners, consecutive samples) than independent random ones
+    roofline["traffic_gbs_at_kernel_time"] = NCU_TRAFFIC_BYTES / (kern_ms / 1e3) / 1e9
+    roofline["traffic_vs_random_read_ceiling"] = roofline["traffic_gbs_at_kernel_time"] / rnd["read_sector_gbs"]
     line["bf16_storage"] = storage_leg(pg, grid, T, imgs, W, dev, torch.bfloat16, args.steps,
                                        args.warmup)
     line["full_training_step"] = full_step_leg(pg, grid, T, imgs, W, dev, args.steps, args.warmup)

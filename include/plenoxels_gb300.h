@@ -340,6 +340,17 @@ int pgb_splat_preview(const float* cells, const int32_t dims[3], float points_di
 int pgb_remove_noise(float* cells, const int32_t dims[3], int32_t kernel_size, double radius,
                      float threshold, int32_t repeats, float* sums_scratch, pgb_stream_t stream);
 
+/* Device-memory probes (no counterpart in the reference): num_reads independent 16 B
+ * loads, or num_updates float4 atomic adds of 1, at pseudo-random 16 B slots of a
+ * 16-byte-aligned device buffer of table_bytes bytes (every slot inside it). Timed by the
+ * caller around the launch, they give the random 32 B sector rate that bounds the render
+ * kernels' cell gathers and gradient scatters. sink: one device float, written only if
+ * the loaded values sum to -1. */
+int pgb_probe_random_reads(const void* table, int64_t table_bytes, int64_t num_reads, uint64_t seed,
+                           float* sink, pgb_stream_t stream);
+int pgb_probe_random_atomics(void* table, int64_t table_bytes, int64_t num_updates, uint64_t seed,
+                             pgb_stream_t stream);
+
 /* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel. */
 int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream);
 

@@ -123,6 +123,8 @@ _SIGNATURES = {
     "pgb_composite_fwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P]),
     "pgb_composite_bwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P, _P]),
     "pgb_fill_zero": (c_int32, [_P, c_int64, _P]),
+    "pgb_probe_random_reads": (c_int32, [_P, c_int64, c_int64, c_uint64, _P, _P]),
+    "pgb_probe_random_atomics": (c_int32, [_P, c_int64, c_int64, c_uint64, _P]),
     "pgb_rgba_to_image": (c_int32, [_P, c_int32, _P, _P]),
     "pgb_splat_size": (c_int32, [POINTER(c_float), c_int32, POINTER(c_int32)]),
     "pgb_splat_preview": (c_int32, [_P, POINTER(c_int32), c_float, POINTER(c_float), c_float, c_int32, c_float,

@@ -24,6 +24,14 @@
 #ifndef PGB_BATCH_GATHER_INLINE
 #define PGB_BATCH_GATHER_INLINE 0
 #endif
+// Resident 256-thread blocks per SM the register allocation must allow.
+#ifndef PGB_BATCH_MIN_BLOCKS
+#define PGB_BATCH_MIN_BLOCKS 3
+#endif
+// Skip the transmittance and adjoint scans of slots with nothing in them (exact).
+#ifndef PGB_SLOT_SKIP
+#define PGB_SLOT_SKIP 1
+#endif
 
 #include "pgb_host.h"
 #include "render.cuh"
@@ -115,7 +123,7 @@ PGB_BATCH_GATHER_ATTR bool batch_sample(const RenderArgs<float>& ra, const Ray<f
 }
 
 template <typename Store, int MODE, int K>
-__global__ void __launch_bounds__(kBatchMaxThreads) batch_train_kernel(const BatchArgs a) {
+__global__ void __launch_bounds__(kBatchMaxThreads, PGB_BATCH_MIN_BLOCKS) batch_train_kernel(const BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   pgb_scene* sc_tab = reinterpret_cast<pgb_scene*>(smem_raw);
   const size_t tab_bytes = ((size_t)a.num_scenes * sizeof(pgb_scene) + 15) & ~(size_t)15;
@@ -223,6 +231,8 @@ __global__ void __launch_bounds__(kBatchMaxThreads) batch_train_kernel(const Bat
       __syncwarp();
 #pragma unroll
       for (int k = K - 1; k >= 0; --k) {
+        // a slot with alpha 0 and nothing to scatter leaves S unchanged (identity maps)
+        if (PGB_SLOT_SKIP && !__any_sync(kFull, bits[k] != 0u || v[k][3] != 0.f)) continue;
         const float al = v[k][3];
         const float G = gpx[0] * v[k][0] + gpx[1] * v[k][1] + gpx[2] * v[k][2] + gpx[3];
         float fa = G * al, fb = 1.f - al;
@@ -234,6 +244,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads) batch_train_kernel(const Bat
         if (bits[k] != 0u) {
           const float w = al * Ts[k];
           float dv[4] = {gpx[0] * w, gpx[1] * w, gpx[2] * w, Ts[k] * (G - S_after)};
+          if (!(dv[0] != 0.f || dv[1] != 0.f || dv[2] != 0.f || dv[3] != 0.f)) continue;
           float nx, ny, nz;
           cs.get(k, lane, nx, ny, nz);
           sample_scatter<float, MODE>(ra.g, grad, nx, ny, nz, dv, bits[k]);

@@ -408,10 +408,21 @@ __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ra
 
 // Exclusive transmittance of every sample of a chunk from the chunk's starting T;
 // returns T after the chunk.
+#ifndef PGB_SLOT_SKIP
+#define PGB_SLOT_SKIP 0  // 1: skip the scans of slots whose 32 samples all have alpha 0
+#endif                   //    (exact; a vote per slot costs more than it saves here)
+#ifndef PGB_SKIP_ZERO_DV
+#define PGB_SKIP_ZERO_DV 1  // skip the scatter of samples whose four partials are all 0
+#endif
+
 template <typename Real, int K>
 __device__ __forceinline__ Real scan_chunk(const Real v[K][4], Real T, int lane, Real Ts[K]) {
 #pragma unroll
   for (int k = 0; k < K; ++k) {
+    if (PGB_SLOT_SKIP && !__any_sync(kFull, v[k][3] != Real(0))) {
+      Ts[k] = T;  // every factor (1 - alpha) is 1: the exact result of the scan
+      continue;
+    }
     const Real incl = warp_incl_prod(Real(1) - v[k][3], lane);
     Real excl = __shfl_up_sync(kFull, incl, 1);
     if (lane == 0) excl = Real(1);
@@ -532,6 +543,8 @@ render_kernel(const RenderArgs<Real> a) {
       __syncwarp();
 #pragma unroll
       for (int k = K - 1; k >= 0; --k) {
+        // a slot with alpha 0 and nothing to scatter leaves S unchanged (identity maps)
+        if (PGB_SLOT_SKIP && !__any_sync(kFull, bits[k] != 0u || v[k][3] != Real(0))) continue;
         const Real al = v[k][3];
         const Real G = gpx[0] * v[k][0] + gpx[1] * v[k][1] + gpx[2] * v[k][2] + gpx[3];
         Real fa = G * al, fb = Real(1) - al;
@@ -551,6 +564,10 @@ render_kernel(const RenderArgs<Real> a) {
             const Real e = (Real)a.beta_eps;
             dv[3] += (Real)(a.beta_w * a.inv_samples) * (Real(1) / (al + e) + Real(1) / (Real(1) - al + e));
           }
+          // behind an opaque sample (T = 0) every partial is 0 and no corner would be written
+          if (PGB_SKIP_ZERO_DV &&
+              !(dv[0] != Real(0) || dv[1] != Real(0) || dv[2] != Real(0) || dv[3] != Real(0)))
+            continue;
           Real nx, ny, nz;
           if (PGB_COORDS_IN_SMEM) {
             cs.get(k, lane, nx, ny, nz);

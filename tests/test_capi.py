@@ -111,6 +111,10 @@ def test_argument_validation_without_launch(lib):
                                 None) == _lib.PGB_ERR_ARG
     assert lib.pgb_wrap_indices(None, 3, None, None) == _lib.PGB_ERR_ARG
     assert lib.pgb_fill_zero(24, 16, None) == _lib.PGB_ERR_ALIGN
+    assert lib.pgb_probe_random_reads(None, 256, 8, 1, 16, None) == _lib.PGB_ERR_ARG
+    assert lib.pgb_probe_random_reads(24, 256, 8, 1, 16, None) == _lib.PGB_ERR_ALIGN
+    assert lib.pgb_probe_random_atomics(16, 8, 8, 1, None) == _lib.PGB_ERR_ARG  # < one slot
+    assert lib.pgb_probe_random_atomics(16, 256, 0, 1, None) == _lib.PGB_OK  # nothing to do
     # even_spread with a non-square ray count
     assert lib.pgb_generate_rays(16, 1, 10, ctypes.c_float(0.5), 16, 4, 4, None, 1, 16, 16, None,
                                  None) == _lib.PGB_ERR_ARG

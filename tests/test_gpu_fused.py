@@ -7,6 +7,7 @@ import pytest
 import torch
 
 import plenoxels_gb300 as pg
+from plenoxels_gb300 import _lib
 import scenes
 from oracle import torch_port as tp
 
@@ -219,3 +220,20 @@ def test_overlapped_gradient_zeroing_gives_the_same_steps():
         assert float(la) == float(lb)
         _grad_close(a.grad, b.grad, rel=1e-6)
     assert len(seen) == 2, "the two gradient buffers alternate"
+
+
+def test_random_access_probes_stay_inside_their_table():
+    """The memory probes behind the roofline report: every atomic lands in the table
+    (its sum is exactly 4 per update) and the read probe completes."""
+    lib = _lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    table = torch.zeros(1000 * 4, device=DEV)  # 1000 slots of 16 B
+    n = 123457
+    _lib.check(lib.pgb_probe_random_atomics(table.data_ptr(), table.numel() * 4, n, 5, stream))
+    assert float(table.double().sum()) == 4.0 * n
+    hit = table.view(-1, 4)[:, 0] > 0
+    assert int(hit.sum()) > 900  # the slots are spread over the whole table
+    sink = torch.zeros(1, device=DEV)
+    _lib.check(lib.pgb_probe_random_reads(table.data_ptr(), table.numel() * 4, n, 6, sink.data_ptr(), stream))
+    torch.cuda.synchronize()
+    assert float(sink) == 0.0
