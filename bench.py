@@ -234,14 +234,14 @@ def random_access_ceiling(pg, dev, reads=1 << 24, reps=5):
         n = reads if kind == "reads" else reads // 4
         ms = []
         for rep in range(reps + 1):
-            _lib.check(lib.pgb_fill_zero(flush.data_ptr(), nbytes, stream))
+            _lib.check(lib.pgb_fill_zero(flush.data_ptr(), nbytes, stream), "pgb_fill_zero")
             e0.record()
             if kind == "reads":
                 st = lib.pgb_probe_random_reads(table.data_ptr(), nbytes, n, 17 + rep, sink.data_ptr(), stream)
             else:
                 st = lib.pgb_probe_random_atomics(table.data_ptr(), nbytes, n, 17 + rep, stream)
             e1.record()
-            _lib.check(st)
+            _lib.check(st, "pgb_probe_random_" + kind)
             torch.cuda.synchronize(dev)
             if rep:
                 ms.append(e0.elapsed_time(e1))

@@ -229,11 +229,11 @@ def test_random_access_probes_stay_inside_their_table():
     stream = torch.cuda.current_stream().cuda_stream
     table = torch.zeros(1000 * 4, device=DEV)  # 1000 slots of 16 B
     n = 123457
-    _lib.check(lib.pgb_probe_random_atomics(table.data_ptr(), table.numel() * 4, n, 5, stream))
+    _lib.check(lib.pgb_probe_random_atomics(table.data_ptr(), table.numel() * 4, n, 5, stream), "atomics")
     assert float(table.double().sum()) == 4.0 * n
     hit = table.view(-1, 4)[:, 0] > 0
     assert int(hit.sum()) > 900  # the slots are spread over the whole table
     sink = torch.zeros(1, device=DEV)
-    _lib.check(lib.pgb_probe_random_reads(table.data_ptr(), table.numel() * 4, n, 6, sink.data_ptr(), stream))
+    _lib.check(lib.pgb_probe_random_reads(table.data_ptr(), table.numel() * 4, n, 6, sink.data_ptr(), stream), "reads")
     torch.cuda.synchronize()
     assert float(sink) == 0.0
