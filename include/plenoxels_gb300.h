@@ -77,6 +77,9 @@ typedef struct {
   float term_threshold;     /* >0: stop a ray once its transmittance falls below this */
   int32_t use_background;   /* 1: output rgb += (1 - alpha) * background (alpha unchanged) */
   float background[3];      /* e.g. 1,1,1 for a white background; the reference has none */
+  int32_t log_transmittance; /* 1: T = exp(compensated sum of log(1 - alpha)) instead of the
+                                reference's product; fp32/BF16 grids with clip only (the
+                                precision form; no counterpart in the reference) */
 } pgb_rays;
 
 /* ---- fused render path (scripts/train.py:142-156 composed with src/ray_sampling.py,

@@ -60,6 +60,7 @@ class PgbRays(Structure):
         ("term_threshold", c_float),
         ("use_background", c_int32),
         ("background", c_float * 3),
+        ("log_transmittance", c_int32),
     ]
 
 

@@ -77,6 +77,10 @@ GridP<Real> grid_params(const pgb_grid* g) {
 int check_rays(const pgb_grid* g, const pgb_rays* r, bool need_target_or_cams) {
   if (!r || r->num_rays < 0 || r->num_samples < 0) return PGB_ERR_ARG;
   if (r->num_samples > kMaxSamples) return PGB_ERR_UNSUPPORTED;
+  if (r->log_transmittance) {
+    if (g->dtype == PGB_F64) return PGB_ERR_UNSUPPORTED;
+    if (!g->clip) return PGB_ERR_ARG;  // log(1 - alpha) needs alpha in [0, 1]
+  }
   if (r->cameras) {
     const pgb_cameras* c = r->cameras;
     if (g->dtype == PGB_F64) return PGB_ERR_UNSUPPORTED;
@@ -121,15 +125,22 @@ RenderArgs<Real> render_args(const pgb_grid* g, const pgb_rays* r) {
 }
 
 template <typename Real>
-int dispatch_render(const pgb_grid* g, RenderArgs<Real>& a, int phase, cudaStream_t s);
+int dispatch_render(const pgb_grid* g, const pgb_rays* r, RenderArgs<Real>& a, int phase,
+                    cudaStream_t s);
 
 template <>
-int dispatch_render<float>(const pgb_grid* g, RenderArgs<float>& a, int phase, cudaStream_t s) {
+int dispatch_render<float>(const pgb_grid* g, const pgb_rays* r, RenderArgs<float>& a, int phase,
+                           cudaStream_t s) {
+  if (r->log_transmittance)
+    return g->dtype == PGB_BF16 ? launch_render_logt_bf16(a, g->mode, phase, s)
+                                : launch_render_logt_f32(a, g->mode, phase, s);
   return g->dtype == PGB_BF16 ? launch_render_bf16(a, g->mode, phase, s)
                               : launch_render_f32(a, g->mode, phase, s);
 }
 template <>
-int dispatch_render<double>(const pgb_grid* g, RenderArgs<double>& a, int phase, cudaStream_t s) {
+int dispatch_render<double>(const pgb_grid* g, const pgb_rays* r, RenderArgs<double>& a, int phase,
+                            cudaStream_t s) {
+  (void)r;  // check_rays rejects the log-sum form for fp64 grids
   return launch_render_f64(a, g->mode, phase, s);
 }
 
@@ -155,7 +166,7 @@ int render_common(const pgb_grid* g, const pgb_rays* r, int phase, void* rgba_ou
   }
   a.loss_w = loss_w;
   a.inv_count = r->num_rays > 0 ? 1.0 / (4.0 * (double)r->num_rays) : std::nan("");
-  return dispatch_render<Real>(g, a, phase, s);
+  return dispatch_render<Real>(g, r, a, phase, s);
 }
 
 }  // namespace

@@ -119,6 +119,7 @@ extern "C" int pgb_render_train_noalloc(const pgb_grid* grid, const pgb_rays* ra
   if (!aligned_to(grid->cells, grid->dtype == PGB_BF16 ? 8 : 16)) return PGB_ERR_ALIGN;
   if (rays->num_rays < 0 || rays->num_samples < 0) return PGB_ERR_ARG;
   if (rays->num_samples > kMaxSamples) return PGB_ERR_UNSUPPORTED;
+  if (rays->log_transmittance) return PGB_ERR_UNSUPPORTED;  // product-scan form only
   // the scratch holds the loss partials of at most PGB_NOALLOC_MAX_RAYS rays per call
   if (rays->num_rays > PGB_NOALLOC_MAX_RAYS) return PGB_ERR_UNSUPPORTED;
   if (rays->cameras) {

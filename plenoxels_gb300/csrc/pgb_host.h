@@ -24,6 +24,9 @@ constexpr int kMaxSamples = kMaxChunks * 32 * 8;
 int launch_render_f32(const RenderArgs<float>& a, int mode, int phase, cudaStream_t s);
 int launch_render_bf16(const RenderArgs<float>& a, int mode, int phase, cudaStream_t s);
 int launch_render_f64(const RenderArgs<double>& a, int mode, int phase, cudaStream_t s);
+// Log-sum transmittance form (fp32 arithmetic over fp32 or BF16 cells).
+int launch_render_logt_f32(const RenderArgs<float>& a, int mode, int phase, cudaStream_t s);
+int launch_render_logt_bf16(const RenderArgs<float>& a, int mode, int phase, cudaStream_t s);
 
 // Slots per lane (K) used for a ray of S samples: one chunk up to 512 samples,
 // 256-sample chunks beyond.

@@ -432,6 +432,51 @@ __device__ __forceinline__ Real scan_chunk(const Real v[K][4], Real T, int lane,
   return T;
 }
 
+// Error-free sum a + b = s + e (Knuth's TwoSum, six additions, no FMA). An infinite sum
+// (an opaque sample: log(1 - 1) = -inf) carries no error term.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  if (isinf(s)) {
+    e = 0.0f;
+    return;
+  }
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Compensated log-sum form of scan_chunk: T_s = exp(sum_{j<s} log(1 - alpha_j)), the sum
+// carried as an unevaluated pair (L + C) across slots and chunks, each warp-scan step an
+// error-free TwoSum whose error joins the compensation term (Kahan-Babuska style). Alpha
+// must lie in [0, 1] (clipped cells): log1p(-alpha) is -inf at alpha = 1 and T is then 0.
+template <int K>
+__device__ __forceinline__ void scan_chunk_log(const float v[K][4], float& L, float& C, int lane,
+                                               float Ts[K]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float a = log1pf(-v[k][3]);
+    float c = 0.0f;
+#pragma unroll
+    for (int d = 1; d < kWarp; d <<= 1) {
+      const float ya = __shfl_up_sync(kFull, a, d), yc = __shfl_up_sync(kFull, c, d);
+      if (lane >= d) {
+        float sum, err;
+        two_sum(ya, a, sum, err);
+        a = sum;
+        c = __fadd_rn(__fadd_rn(c, yc), err);
+      }
+    }
+    float ea = __shfl_up_sync(kFull, a, 1), ec = __shfl_up_sync(kFull, c, 1);
+    if (lane == 0) ea = ec = 0.0f;
+    float sum, err;
+    two_sum(L, ea, sum, err);
+    Ts[k] = isinf(sum) ? 0.0f : expf(__fadd_rn(sum, __fadd_rn(__fadd_rn(C, ec), err)));
+    const float ta = __shfl_sync(kFull, a, kWarp - 1), tc = __shfl_sync(kFull, c, kWarp - 1);
+    two_sum(L, ta, sum, err);
+    L = sum;
+    C = isinf(sum) ? 0.0f : __fadd_rn(__fadd_rn(C, tc), err);
+  }
+}
+
 // v[i] for a runtime i in [0,4) without indexing a register array dynamically.
 template <typename Real>
 __device__ __forceinline__ Real pick4(const Real v[4], int i) {
@@ -443,9 +488,12 @@ constexpr int render_smem_bytes(int warps_per_block) {
   return CoordStage<Real, K>::kBytesPerWarp * warps_per_block;
 }
 
-template <typename Real, typename Store, int MODE, int K, int PHASE>
+// LOGT: transmittance as the compensated log-sum (scan_chunk_log, fp32 only) instead of
+// the reference's product scan.
+template <typename Real, typename Store, int MODE, int K, int PHASE, bool LOGT = false>
 __global__ void __launch_bounds__(kRenderThreads, PGB_RENDER_MIN_BLOCKS)
 render_kernel(const RenderArgs<Real> a) {
+  static_assert(!LOGT || sizeof(Real) == 4, "log-sum transmittance is an fp32 form");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr bool ADJ = PHASE != kForward;
   const int lane = threadIdx.x & (kWarp - 1);
@@ -475,12 +523,22 @@ render_kernel(const RenderArgs<Real> a) {
     Real acc[4] = {Real(0), Real(0), Real(0), Real(0)};
     Real T = Real(1);
     Real Tstart = Real(1);  // lane c: transmittance at the start of chunk c
+    float LT = 0.0f, LC = 0.0f, LTstart = 0.0f, LCstart = 0.0f;  // LOGT: log T = LT + LC
     int last = -1;          // last composited chunk (-1: none, e.g. zero samples)
     for (int c = 0; c < nchunks; ++c) {
-      if (lane == c) Tstart = T;
+      if (lane == c) {
+        Tstart = T;
+        LTstart = LT;
+        LCstart = LC;
+      }
       __syncwarp();
       gather_chunk<Real, Store, MODE, K, ADJ>(a, ray, c, lane, v, bits, cs);
-      T = scan_chunk<Real, K>(v, T, lane, Ts);
+      if constexpr (LOGT) {
+        scan_chunk_log<K>(v, LT, LC, lane, Ts);
+        T = isinf(LT) ? Real(0) : (Real)expf(LT + LC);
+      } else {
+        T = scan_chunk<Real, K>(v, T, lane, Ts);
+      }
 #pragma unroll
       for (int k = 0; k < K; ++k) {
         const Real w = v[k][3] * Ts[k];
@@ -538,7 +596,12 @@ render_kernel(const RenderArgs<Real> a) {
       if (c != last) {
         __syncwarp();
         gather_chunk<Real, Store, MODE, K, true>(a, ray, c, lane, v, bits, cs);
-        scan_chunk<Real, K>(v, __shfl_sync(kFull, Tstart, c), lane, Ts);
+        if constexpr (LOGT) {
+          float l = __shfl_sync(kFull, LTstart, c), lc = __shfl_sync(kFull, LCstart, c);
+          scan_chunk_log<K>(v, l, lc, lane, Ts);
+        } else {
+          scan_chunk<Real, K>(v, __shfl_sync(kFull, Tstart, c), lane, Ts);
+        }
       }
       __syncwarp();
 #pragma unroll

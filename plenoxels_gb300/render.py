@@ -26,8 +26,17 @@ def _mode(mode) -> int:
     return MODES[mode]
 
 
+TRANSMITTANCE = {"product": 0, "logsum": 1}
+
+
+def _transmittance(name: str) -> int:
+    if name not in TRANSMITTANCE:
+        raise ValueError(f"transmittance must be 'product' or 'logsum', got {name!r}")
+    return TRANSMITTANCE[name]
+
+
 def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, seed, term_threshold,
-               cameras=None, background=None) -> PgbRays:
+               cameras=None, background=None, log_t=0) -> PgbRays:
     r = PgbRays()
     r.origins = ptr(origins)
     r.dirs = ptr(dirs)
@@ -41,6 +50,7 @@ def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, see
     if background is not None:
         r.use_background = 1
         r.background[:] = [float(v) for v in background]
+    r.log_transmittance = int(log_t)
     return r
 
 
@@ -64,7 +74,7 @@ class _RenderRays(torch.autograd.Function):
         gdesc = _lib.make_grid(grid, cfg["origin"], cfg["points_distance"], cfg["mode"], cfg["clip"])
         rdesc = _rays_desc(origins, dirs, R, cfg["num_samples"], cfg["delta_step"],
                            cfg["stratified"], cfg["seed"], cfg["term_threshold"],
-                           background=cfg["background"])
+                           background=cfg["background"], log_t=cfg["log_t"])
         check(lib.pgb_render_fwd(gdesc, rdesc, ptr(rgba), stream_of(grid)), "render_rays")
         ctx.save_for_backward(grid, origins, dirs)
         ctx.cfg = cfg
@@ -82,20 +92,22 @@ class _RenderRays(torch.autograd.Function):
         gdesc = _lib.make_grid(grid, cfg["origin"], cfg["points_distance"], cfg["mode"], cfg["clip"])
         rdesc = _rays_desc(origins, dirs, origins.shape[0], cfg["num_samples"], cfg["delta_step"],
                            cfg["stratified"], cfg["seed"], cfg["term_threshold"],
-                           background=cfg["background"])
+                           background=cfg["background"], log_t=cfg["log_t"])
         check(lib.pgb_render_bwd(gdesc, rdesc, ptr(d_rgba), ptr(grad), s), "render_rays backward")
         return grad, None, None, None
 
 
 def render_rays(grid, origins, dirs, delta_step, num_samples, points_distance, grid_min=None,
                 mode="trilinear", clip=True, stratified=False, seed=0, term_threshold=0.0,
-                background=None):
+                background=None, transmittance="product"):
     """Premultiplied RGBA [R,4] of rays through a dense [X,Y,Z,4] grid.
 
     Samples sit at origins + dirs * (delta_step * k), k = 1..num_samples (minus a
     per-sample jitter in [0,1) when stratified); grid_min is the world position of cell
     (0,0,0) (default: generate_grid's layout, grid_origin()). background (3 values, e.g. white)
-    composites rgb over it: rgb + (1 - alpha) * background. Differentiable in grid."""
+    composites rgb over it: rgb + (1 - alpha) * background. transmittance "logsum" evaluates
+    T = exp(compensated sum of log(1 - alpha)) instead of the reference's running product
+    (fp32/BF16 grids, clip=True). Differentiable in grid."""
     require_cuda(grid, origins, dirs)
     _check_rays(grid, origins, dirs)
     if grid_min is None:
@@ -104,7 +116,8 @@ def render_rays(grid, origins, dirs, delta_step, num_samples, points_distance, g
                mode=_mode(mode), clip=bool(clip), num_samples=int(num_samples),
                delta_step=float(delta_step), stratified=bool(stratified), seed=int(seed),
                term_threshold=float(term_threshold),
-               background=None if background is None else tuple(float(v) for v in background))
+               background=None if background is None else tuple(float(v) for v in background),
+               log_t=_transmittance(transmittance))
     return _RenderRays.apply(grid.contiguous(), origins.contiguous(), dirs.contiguous(), cfg)
 
 
@@ -173,6 +186,7 @@ class FusedTrainStep:
 
     beta > 0 adds the reference's beta loss on the sampled opacities (scripts/train.py:
     170-177) in the same launch; ``self.losses`` holds [weighted MSE, beta term].
+    transmittance="logsum" selects the compensated log-sum transmittance (see render_rays).
 
     The gradient goes to ``self.grad`` (fp32 for fp32/bf16 grids, fp64 for fp64 grids),
     which is also attached as ``grid.grad`` when the dtypes agree, so a torch optimizer
@@ -188,7 +202,8 @@ class FusedTrainStep:
 
     def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
                  grid_min=None, clip=True, stratified=False, seed=0, term_threshold=0.0,
-                 loss_weight=1.0, overlap_zero=False, beta=0.0, beta_eps=1e-4, background=None):
+                 loss_weight=1.0, overlap_zero=False, beta=0.0, beta_eps=1e-4, background=None,
+                 transmittance="product"):
         require_cuda(grid)
         if grid.dim() != 4 or grid.shape[-1] != 4 or not grid.is_contiguous():
             raise ValueError("grid must be a contiguous [X,Y,Z,4] tensor")
@@ -208,6 +223,7 @@ class FusedTrainStep:
         self.beta = float(beta)
         self.beta_eps = float(beta_eps)
         self.background = None if background is None else tuple(float(v) for v in background)
+        self.log_t = _transmittance(transmittance)
         lib = _lib.load()
         dev = grid.device
         self.workspace = torch.zeros(lib.pgb_train_workspace_bytes(), dtype=torch.uint8, device=dev)
@@ -292,7 +308,8 @@ class FusedTrainStep:
         if target.shape != (origins.shape[0], 4) or target.dtype != self.real:
             raise ValueError(f"target must be [R,4] {self.real}")
         rdesc = _rays_desc(origins, dirs, origins.shape[0], self.num_samples, self.delta_step,
-                           self.stratified, self.seed, self.term_threshold, background=self.background)
+                           self.stratified, self.seed, self.term_threshold, background=self.background,
+                           log_t=self.log_t)
         return self._launch(rdesc, target.contiguous(), rgba_out, zero_grad)
 
     def step_cameras(self, transforms, images, camera_angle_x, num_rays, ray_seed, near=0.0,
@@ -303,5 +320,6 @@ class FusedTrainStep:
         cams = _camera_desc(transforms, images, camera_angle_x, ray_seed, near)
         self._cams = cams  # keep alive for the call
         rdesc = _rays_desc(None, None, num_rays, self.num_samples, self.delta_step, self.stratified,
-                           self.seed, self.term_threshold, cameras=cams, background=self.background)
+                           self.seed, self.term_threshold, cameras=cams, background=self.background,
+                           log_t=self.log_t)
         return self._launch(rdesc, None, rgba_out, zero_grad)
