@@ -219,6 +219,17 @@ int pgb_tv_grad(const float* cells, const int32_t dims[3], const double* sumsq, 
 int pgb_adam_step(float* param, float* grad, float* exp_avg, float* exp_avg_sq,
                   float* abs_grad_accum, int64_t count, double lr, double beta1, double beta2,
                   double eps, int64_t step, int32_t zero_grad, pgb_stream_t stream);
+/* pgb_adam_step on grad + the gradient of tv_weight * sqrt(Q) (Q from pgb_tv_sumsq of
+ * param_in, the TV term of scripts/train.py:44-65, :163-165), the stencil evaluated as
+ * pgb_tv_grad does, in the same pass as the update: the TV gradient pass and the Adam pass
+ * of scripts/train.py:163-165, :182 fused. param_in is the [X,Y,Z,4] grid before the step,
+ * param_out (a different buffer) receives it after; the moments, the accumulator and the
+ * cleared gradient are updated in place. No counterpart in the reference (it runs TV
+ * backward and optimizer.step() as separate passes). */
+int pgb_adam_tv_step(const float* param_in, float* param_out, float* grad, float* exp_avg,
+                     float* exp_avg_sq, float* abs_grad_accum, const int32_t dims[3],
+                     const double* tv_sumsq, float tv_weight, double lr, double beta1, double beta2,
+                     double eps, int64_t step, int32_t zero_grad, pgb_stream_t stream);
 
 /* src/grid_functions.py:173-181 average_pool3d_grid (scripts/train.py:108-123): average of
  * a cubic window of `window` cells, stride `stride`, no padding, of a contiguous fp32

@@ -104,6 +104,8 @@ _SIGNATURES = {
     "pgb_tv_grad": (c_int32, [_P, POINTER(c_int32), _P, c_float, _P, _P]),
     "pgb_adam_step": (c_int32, [_P, _P, _P, _P, _P, c_int64, c_double, c_double, c_double, c_double,
                                 c_int64, c_int32, _P]),
+    "pgb_adam_tv_step": (c_int32, [_P, _P, _P, _P, _P, _P, POINTER(c_int32), _P, c_float, c_double, c_double,
+                                   c_double, c_double, c_int64, c_int32, _P]),
     "pgb_avg_pool3d_shape": (c_int32, [POINTER(c_int32), c_int32, c_int32, POINTER(c_int32), POINTER(c_int64)]),
     "pgb_avg_pool3d_fwd": (c_int32, [_P, POINTER(c_int32), c_int32, c_int32, _P, _P, _P]),
     "pgb_avg_pool3d_bwd": (c_int32, [_P, POINTER(c_int32), c_int32, c_int32, _P, _P, _P]),

@@ -8,6 +8,8 @@
 //  pgb_tv_grad   grad += w / sqrt(Q) * sum_{j in N(i)} (v_i - v_j), the gradient of w*sqrt(Q)
 //  pgb_adam_step torch.optim.Adam's update (lerp of the first moment, bias corrections),
 //                accum += |grad|, grad = 0, in one pass
+//  pgb_adam_tv_step  the two passes above fused: Adam on grad + the TV gradient, written
+//                to a second parameter buffer
 #include <algorithm>
 #include <cmath>
 
@@ -163,6 +165,77 @@ __global__ void adam_kernel(float4* __restrict__ p, float4* __restrict__ g, floa
   }
 }
 
+// Adam with the TV gradient added on the fly: the tv_grad_kernel stencil (same neighbour
+// order, same fp32 expression) feeding adam_one, over the (z-blocks, Y, x-chunks) grid of
+// the TV kernels. Neighbours are read from pin while cells are updated, so the update goes
+// to pout (a different buffer): one pass instead of the TV gradient's read-modify-write of
+// grad followed by Adam.
+__global__ void __launch_bounds__(kTvThreads) adam_tv_kernel(
+    const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ g,
+    float4* __restrict__ mo, float4* __restrict__ so, float4* __restrict__ acc, int X, int Y,
+    int Z, const double* __restrict__ sumsq, float weight, AdamConst k, int zero_grad) {
+  const double q = sumsq[0];
+  const bool tv = q > 0.0;  // a constant grid: no TV term (as tv_grad_kernel)
+  const float c = tv ? (float)((double)weight / sqrt(q)) : 0.f;
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  const int XL = (X + gridDim.z - 1) / gridDim.z;
+  const int x0 = blockIdx.z * XL, x1 = min(X, x0 + XL);
+  if (z >= Z || x0 >= x1) return;
+  const int64_t YZ = (int64_t)Y * Z;
+  int64_t i = (int64_t)x0 * YZ + (int64_t)y * Z + z;
+  float4 prev = x0 > 0 ? __ldg(pin + i - YZ) : make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 m = __ldg(pin + i);
+  for (int x = x0; x < x1; ++x, i += YZ) {
+    const float4 next = x + 1 < X ? __ldg(pin + i + YZ) : m;
+    float4 Gr = g[i];
+    if (tv) {
+      float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+      auto add = [&](float4 nb) {
+        d.x += m.x - nb.x; d.y += m.y - nb.y; d.z += m.z - nb.z; d.w += m.w - nb.w;
+      };
+      if (z > 0) add(__ldg(pin + i - 1));
+      if (z + 1 < Z) add(__ldg(pin + i + 1));
+      if (y > 0) add(__ldg(pin + i - Z));
+      if (y + 1 < Y) add(__ldg(pin + i + Z));
+      if (x > 0) add(prev);
+      if (x + 1 < X) add(next);
+      Gr.x += c * d.x; Gr.y += c * d.y; Gr.z += c * d.z; Gr.w += c * d.w;
+    }
+    float4 P = m, M = mo[i], S = so[i];
+    float4 A;
+    A.x = adam_one(P.x, Gr.x, M.x, S.x, k);
+    A.y = adam_one(P.y, Gr.y, M.y, S.y, k);
+    A.z = adam_one(P.z, Gr.z, M.z, S.z, k);
+    A.w = adam_one(P.w, Gr.w, M.w, S.w, k);
+    pout[i] = P;
+    mo[i] = M;
+    so[i] = S;
+    if (acc) {
+      float4 a = acc[i];
+      a.x += A.x; a.y += A.y; a.z += A.z; a.w += A.w;
+      acc[i] = a;
+    }
+    if (zero_grad) g[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    prev = m;
+    m = next;
+  }
+}
+
+AdamConst adam_const(double lr, double beta1, double beta2, double eps, int64_t step) {
+  // torch.optim.Adam (non-capturable path): bias corrections in double on the host
+  const double bc1 = 1.0 - std::pow(beta1, (double)step);
+  const double bc2 = 1.0 - std::pow(beta2, (double)step);
+  AdamConst k;
+  k.one_minus_b1 = (float)(1.0 - beta1);
+  k.b2 = (float)beta2;
+  k.one_minus_b2 = (float)(1.0 - beta2);
+  k.step_size = (float)(lr / bc1);
+  k.inv_bc2_sqrt = (float)(1.0 / std::sqrt(bc2));
+  k.eps = (float)eps;
+  return k;
+}
+
 inline unsigned stream_blocks(int64_t n) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
 }
@@ -215,21 +288,34 @@ int pgb_adam_step(float* param, float* grad, float* exp_avg, float* exp_avg_sq, 
   if (!al16(param) || !al16(grad) || !al16(exp_avg) || !al16(exp_avg_sq) ||
       (abs_grad_accum && !al16(abs_grad_accum)))
     return PGB_ERR_ALIGN;
-  // torch.optim.Adam (non-capturable path): bias corrections in double on the host
-  const double bc1 = 1.0 - std::pow(beta1, (double)step);
-  const double bc2 = 1.0 - std::pow(beta2, (double)step);
-  AdamConst k;
-  k.one_minus_b1 = (float)(1.0 - beta1);
-  k.b2 = (float)beta2;
-  k.one_minus_b2 = (float)(1.0 - beta2);
-  k.step_size = (float)(lr / bc1);
-  k.inv_bc2_sqrt = (float)(1.0 / std::sqrt(bc2));
-  k.eps = (float)eps;
+  const AdamConst k = adam_const(lr, beta1, beta2, eps, step);
   const int64_t n4 = count / 4;
   adam_kernel<<<stream_blocks(n4), 256, 0, stream>>>(
       reinterpret_cast<float4*>(param), reinterpret_cast<float4*>(grad),
       reinterpret_cast<float4*>(exp_avg), reinterpret_cast<float4*>(exp_avg_sq),
       reinterpret_cast<float4*>(abs_grad_accum), n4, k, zero_grad ? 1 : 0);
+  return after_launch();
+}
+
+int pgb_adam_tv_step(const float* param_in, float* param_out, float* grad, float* exp_avg,
+                     float* exp_avg_sq, float* abs_grad_accum, const int32_t dims[3],
+                     const double* tv_sumsq, float tv_weight, double lr, double beta1, double beta2,
+                     double eps, int64_t step, int32_t zero_grad, pgb_stream_t stream) {
+  if (!dims || step < 1) return PGB_ERR_ARG;
+  if (dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return PGB_ERR_ARG;
+  if (!param_in || !param_out || !grad || !exp_avg || !exp_avg_sq || !tv_sumsq) return PGB_ERR_ARG;
+  if (param_in == param_out) return PGB_ERR_ARG;  // neighbours are read while cells are updated
+  if (!al16(param_in) || !al16(param_out) || !al16(grad) || !al16(exp_avg) || !al16(exp_avg_sq) ||
+      (abs_grad_accum && !al16(abs_grad_accum)))
+    return PGB_ERR_ALIGN;
+  if (dims[1] > 65535) return PGB_ERR_UNSUPPORTED;
+  const AdamConst k = adam_const(lr, beta1, beta2, eps, step);
+  const dim3 grid((dims[2] + kTvThreads - 1) / kTvThreads, dims[1], std::min(dims[0], kTvXChunks));
+  adam_tv_kernel<<<grid, kTvThreads, 0, stream>>>(
+      reinterpret_cast<const float4*>(param_in), reinterpret_cast<float4*>(param_out),
+      reinterpret_cast<float4*>(grad), reinterpret_cast<float4*>(exp_avg),
+      reinterpret_cast<float4*>(exp_avg_sq), reinterpret_cast<float4*>(abs_grad_accum), dims[0],
+      dims[1], dims[2], tv_sumsq, tv_weight, k, zero_grad ? 1 : 0);
   return after_launch();
 }
 

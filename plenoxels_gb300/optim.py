@@ -57,3 +57,29 @@ class FusedAdam:
                                         ptr(self.exp_avg_sq), ptr(self.abs_grad), self.grid.numel(),
                                         self.lr, self.betas[0], self.betas[1], self.eps,
                                         self.step_count, 1 if zero_grad else 0, s), "adam step")
+
+    @torch.no_grad()
+    def step_tv(self, grad, weight, out, zero_grad=True):
+        """add_tv on the optimised grid followed by step, in two passes instead of three:
+        the TV loss value (one reduction over the grid), then Adam on grad + the TV gradient
+        with the stencil evaluated in the update pass. The updated grid is written to
+        ``out`` (a buffer of the grid's shape, not the grid itself: a cell's neighbours are
+        read while cells are updated), which becomes ``self.grid``; the previous grid
+        tensor is left holding the pre-step values. Returns weight * tv_loss as a device
+        scalar."""
+        g = self.grid
+        if out.shape != g.shape or out.dtype != g.dtype or not out.is_contiguous() or out.data_ptr() == g.data_ptr():
+            raise ValueError("out must be a separate contiguous float32 buffer of the grid's shape")
+        if grad is None or grad.shape != g.shape or grad.dtype != torch.float32:
+            raise ValueError("step_tv needs the grid's float32 gradient")
+        lib = _lib.load()
+        s = torch.cuda.current_stream(g.device).cuda_stream
+        dims = _lib.dims3(g.shape)
+        check(lib.pgb_tv_sumsq(ptr(g), dims, ptr(self.tv_sumsq), ptr(self._tv_ws), s), "tv loss")
+        self.step_count += 1
+        check(lib.pgb_adam_tv_step(ptr(g), ptr(out), ptr(grad), ptr(self.exp_avg), ptr(self.exp_avg_sq),
+                                   ptr(self.abs_grad), dims, ptr(self.tv_sumsq), float(weight), self.lr,
+                                   self.betas[0], self.betas[1], self.eps, self.step_count,
+                                   1 if zero_grad else 0, s), "adam + tv step")
+        self.grid = out
+        return float(weight) * self.tv_sumsq.sqrt()

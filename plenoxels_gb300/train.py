@@ -4,6 +4,12 @@ Per step: rays from the cameras and images (in-kernel) or given, forward + MSE +
 loss + backward in one launch (FusedTrainStep), the TV gradient (two passes) when
 enabled, and one Adam pass that also accumulates |grad| and clears the gradient.
 
+With the TV term on the full grid (no pooling), the TV gradient is not a pass of its own:
+Adam evaluates its stencil while updating (FusedAdam.step_tv), which needs the update
+written to a second grid buffer. The trainer then alternates two buffers, and
+``trainer.grid`` is always the current one (fuse_tv=False keeps one buffer, updated in
+place, at the cost of the separate TV gradient pass).
+
 Progressive growing (scripts/train.py:91-123): while the schedule's receptive field r is
 above 1, the step renders the grid average-pooled with window r and stride max(1, r//4)
 (pitch points_distance * stride, origin at the coordinate of cell r//2), and the pooled
@@ -30,8 +36,11 @@ STEPS_PER_FIELD = 5                       # scripts/train.py:92
 class Trainer:
     def __init__(self, grid, points_distance, num_samples, delta_step, lr, tv=0.0, beta=0.0,
                  mode="nearest", betas=(0.9, 0.999), eps=1e-8, stratified=False, seed=0,
-                 progressive_growing=False, fields=None, steps_per_field=STEPS_PER_FIELD):
+                 progressive_growing=False, fields=None, steps_per_field=STEPS_PER_FIELD,
+                 fuse_tv=True):
         self.grid = grid
+        self.fuse_tv = bool(fuse_tv)
+        self._spare = None  # the second grid buffer of the fused TV + Adam pass
         self.points_distance = float(points_distance)
         self.cfg = dict(num_samples=num_samples, delta_step=delta_step, mode=mode,
                         stratified=stratified, seed=seed, beta=beta)
@@ -84,6 +93,17 @@ class Trainer:
         self.losses[0] = render_step.losses[0]
         self.losses[2] = render_step.losses[1] if self.beta != 0.0 else 0.0
         self.losses[1] = 0.0
+        if self.tv > 0.0 and r < 19 and self.fuse_tv and r <= 1:
+            # TV on the full grid: its gradient is evaluated inside the Adam pass, which
+            # writes the new grid to the spare buffer; the buffers then swap roles
+            if self._spare is None:
+                self._spare = torch.empty_like(self.grid)
+            old = self.grid
+            self.losses[1] = self.opt.step_tv(full_grad, self.tv, self._spare)
+            self.grid, self._spare = self._spare, old
+            self.render.grid = self.grid
+            self.step_index += 1
+            return self.losses
         if self.tv > 0.0 and r < 19:
             self.losses[1] = self.opt.add_tv(tv_grad, self.tv, grid=tv_grid)
         if r > 1:

@@ -237,3 +237,89 @@ def test_random_access_probes_stay_inside_their_table():
     _lib.check(lib.pgb_probe_random_reads(table.data_ptr(), table.numel() * 4, n, 6, sink.data_ptr(), stream), "reads")
     torch.cuda.synchronize()
     assert float(sink) == 0.0
+
+
+def _parity(grid, o, d, target, S, delta, pd, gmin, mode, strat=False, seed=9):
+    """Indices bit-exact, forward within 1e-5, gradients within 1e-4 of the largest entry,
+    through both the autograd path and the fused training step."""
+    jitter = tp.jitter_for(seed, o.shape[0], S) if strat else None
+    g_ref = grid.clone().requires_grad_(True)
+    px_ref = tp.render(g_ref, o, d, S, delta, gmin, pd, mode, True, jitter)
+    idx_ref, inb_ref = tp.sample_indices(o, d, S, delta, gmin, pd, grid.shape, mode, jitter)
+    loss_ref = torch.nn.functional.mse_loss(px_ref, target)
+    loss_ref.backward()
+    gmin = tuple(float(x) for x in gmin)
+    g = grid.to(DEV).requires_grad_(True)
+    od, dd = o.to(DEV), d.to(DEV)
+    idx, inb = pg.render_sample_indices(g, od, dd, delta, S, pd, grid_min=gmin, mode=mode,
+                                        stratified=strat, seed=seed)
+    np.testing.assert_array_equal(idx.cpu().numpy().reshape(-1), idx_ref.numpy().reshape(-1))
+    np.testing.assert_array_equal(inb.cpu().numpy().reshape(-1), inb_ref.numpy())
+    px = pg.render_rays(g, od, dd, delta, S, pd, grid_min=gmin, mode=mode, stratified=strat, seed=seed)
+    np.testing.assert_allclose(px.detach().cpu().numpy(), px_ref.detach().numpy(), rtol=1e-5, atol=2e-6)
+    torch.nn.functional.mse_loss(px, target.to(DEV)).backward()
+    _grad_close(g.grad, g_ref.grad)
+    step = pg.FusedTrainStep(g.detach(), pd, S, delta, mode=mode, grid_min=gmin, stratified=strat, seed=seed)
+    loss = step.step_rays(od, dd, target.to(DEV))
+    np.testing.assert_allclose(float(loss), float(loss_ref), rtol=1e-5)
+    _grad_close(step.grad, g_ref.grad)
+    return px_ref, g_ref.grad
+
+
+@pytest.mark.parametrize("mode", ["nearest", "trilinear"])
+def test_non_cubic_grid_matches_oracle(mode):
+    """X != Y != Z (the kernels index with all three extents; the reference's own grids
+    are cubic but nothing in the path assumes it)."""
+    g = torch.Generator().manual_seed(31)
+    grid = torch.rand(20, 28, 12, 4, generator=g) * 1.2 - 0.1   # some channels outside [0,1]
+    grid[..., 3] *= 0.1  # translucent enough that most samples carry gradient
+    pd = 0.11
+    gmin = tp.grid_min(grid.shape, pd)
+    T = torch.from_numpy(scenes.make_cameras(3, 32))
+    imgs = torch.from_numpy(scenes.make_images(3, 16, 16, 33))
+    o, d, target = tp.camera_batch(T, 0.691, imgs, 240, 34, 2.0)
+    _parity(grid, o, d, target, 96, 4.0 / 96, pd, gmin, mode)
+
+
+def test_maximum_samples_per_ray_matches_oracle():
+    """8192 samples per ray (32 chunks of 256, the largest the kernels take), stratified."""
+    grid = torch.from_numpy(scenes.make_grid(16, 3, 41, amp=(0.05, 0.3)))
+    pd = scenes.points_distance(16)
+    gmin = tp.grid_min(grid.shape, pd)
+    T = torch.from_numpy(scenes.make_cameras(2, 42))
+    imgs = torch.from_numpy(scenes.make_images(2, 16, 16, 43))
+    o, d, target = tp.camera_batch(T, 0.691, imgs, 12, 44, 2.0)
+    S = 8192
+    _parity(grid, o, d, target, S, 4.0 / S, pd, gmin, "trilinear", strat=True)
+    with pytest.raises(NotImplementedError):
+        pg.render_rays(grid.to(DEV), o.to(DEV), d.to(DEV), 4.0 / S, S + 1, pd)
+
+
+@pytest.mark.parametrize("side", [1, 2])
+def test_tiny_grids_match_oracle(side):
+    """One- and two-cell grids: every trilinear ceil corner wraps to index 0."""
+    g = torch.Generator().manual_seed(50 + side)
+    grid = torch.rand(side, side, side, 4, generator=g)
+    grid[..., 3] *= 0.1
+    pd = 1.5 / side
+    gmin = tp.grid_min(grid.shape, pd)
+    o = torch.tensor([[-2.0, 0.1, 0.05], [0.2, -2.0, 0.3], [0.01, 0.02, -2.0]]).repeat(8, 1)
+    o = o + 0.05 * torch.rand(o.shape, generator=g)
+    d = torch.nn.functional.normalize(-o + 0.1 * torch.rand(o.shape, generator=g), dim=1)
+    target = torch.rand(o.shape[0], 4, generator=g)
+    for mode in ("nearest", "trilinear"):
+        _parity(grid, o, d, target, 64, 4.0 / 64, pd, gmin, mode)
+
+
+def test_rays_that_miss_the_grid():
+    """Every sample outside the box: RGBA 0, loss = mean(target^2), no gradient."""
+    grid = torch.rand(16, 16, 16, 4, device=DEV)
+    o = torch.tensor([[5.0, 5.0, 5.0], [-5.0, 0.0, 0.0]], device=DEV)
+    d = torch.tensor([[0.0, 0.0, 1.0], [-1.0, 0.0, 0.0]], device=DEV)
+    target = torch.rand(2, 4, device=DEV)
+    step = pg.FusedTrainStep(grid, 0.2, 128, 0.05)
+    loss = step.step_rays(o, d, target)
+    assert abs(float(loss) - float((target ** 2).mean())) <= 1e-7
+    assert float(step.grad.abs().sum()) == 0.0
+    px = pg.render_rays(grid, o, d, 0.05, 128, 0.2)
+    assert float(px.abs().sum()) == 0.0

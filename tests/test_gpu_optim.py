@@ -105,6 +105,29 @@ def test_training_steps_follow_the_reference_loop():
         np.testing.assert_allclose(losses.numpy(), [float(mse), float(tvl), float(bl)], rtol=1e-4)
     # Adam turns tiny gradient differences into step-size differences on cells whose
     # gradient is ~0; the grids agree to a few optimiser steps at most
-    diff = (grid.cpu() - ref.detach()).abs()
+    diff = (trainer.grid.cpu() - ref.detach()).abs()
     assert float(diff.max()) <= 5 * lr
     assert float((diff > 1e-5).float().mean()) < 0.01
+
+
+def test_fused_tv_adam_pass_equals_the_separate_passes():
+    """The TV gradient evaluated inside the Adam pass (two grid buffers) gives bit-identical
+    grids, moments, accumulators and losses to the TV gradient pass followed by Adam."""
+    side, S, R = 20, 48, 300
+    grid0 = torch.from_numpy(scenes.make_grid(side, 3, 91, amp=(0.2, 1.5))).to(DEV)
+    T = torch.from_numpy(scenes.make_cameras(3, 92))
+    imgs = torch.from_numpy(scenes.make_images(3, 8, 8, 93))
+    pd, delta = scenes.points_distance(side), 4.0 / S
+    runs = {}
+    for fuse in (True, False):
+        tr = Trainer(grid0.clone(), pd, S, delta, 0.0075, tv=1e-3, beta=5e-3, mode="trilinear",
+                     fuse_tv=fuse)
+        losses = []
+        for i in range(4):
+            o, d, tgt = tp.camera_batch(T, 0.691, imgs, R, 120 + i, 2.0)
+            losses.append(tr.step_rays(o.to(DEV), d.to(DEV), tgt.to(DEV)).cpu().clone())
+        runs[fuse] = (tr.grid.cpu(), tr.opt.exp_avg.cpu(), tr.opt.exp_avg_sq.cpu(), tr.opt.abs_grad.cpu(),
+                      torch.stack(losses))
+    for a, b in zip(runs[True], runs[False]):
+        assert torch.equal(a, b)
+    assert not torch.equal(runs[True][0], grid0.cpu())
