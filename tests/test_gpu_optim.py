@@ -111,23 +111,48 @@ def test_training_steps_follow_the_reference_loop():
 
 
 def test_fused_tv_adam_pass_equals_the_separate_passes():
-    """The TV gradient evaluated inside the Adam pass (two grid buffers) gives bit-identical
-    grids, moments, accumulators and losses to the TV gradient pass followed by Adam."""
+    """On the same gradient, the TV gradient evaluated inside the Adam pass (two grid
+    buffers) gives bit-identical grids, moments, accumulators and TV values to the TV
+    gradient pass followed by Adam; over whole training steps (whose gradients are summed
+    by atomics in a run-dependent order) the two trainers agree to rounding."""
+    from plenoxels_gb300.optim import FusedAdam
+    g = torch.Generator(device=DEV).manual_seed(95)
+    grid0 = torch.rand(20, 28, 12, 4, generator=g, device=DEV)
+    opts = {fuse: FusedAdam(grid0.clone(), 0.0075) for fuse in (True, False)}
+    spare = torch.empty_like(grid0)
+    for i in range(3):
+        grad = 1e-2 * torch.randn(grid0.shape, generator=g, device=DEV)
+        ga, gb = grad.clone(), grad.clone()
+        old = opts[True].grid
+        tv_a = opts[True].step_tv(ga, 1e-3, spare)
+        spare = old
+        tv_b = opts[False].add_tv(gb, 1e-3)
+        opts[False].step(gb)
+        assert torch.equal(tv_a, tv_b)
+        assert float(ga.abs().sum()) == 0.0 and float(gb.abs().sum()) == 0.0
+    a, b = opts[True], opts[False]
+    for x, y in ((a.grid, b.grid), (a.exp_avg, b.exp_avg), (a.exp_avg_sq, b.exp_avg_sq),
+                 (a.abs_grad, b.abs_grad)):
+        assert torch.equal(x, y)
+    assert not torch.equal(a.grid, grid0)
+    # whole steps through Trainer
     side, S, R = 20, 48, 300
-    grid0 = torch.from_numpy(scenes.make_grid(side, 3, 91, amp=(0.2, 1.5))).to(DEV)
+    gridt = torch.from_numpy(scenes.make_grid(side, 3, 91, amp=(0.2, 1.5))).to(DEV)
     T = torch.from_numpy(scenes.make_cameras(3, 92))
     imgs = torch.from_numpy(scenes.make_images(3, 8, 8, 93))
     pd, delta = scenes.points_distance(side), 4.0 / S
     runs = {}
     for fuse in (True, False):
-        tr = Trainer(grid0.clone(), pd, S, delta, 0.0075, tv=1e-3, beta=5e-3, mode="trilinear",
+        tr = Trainer(gridt.clone(), pd, S, delta, 0.0075, tv=1e-3, beta=5e-3, mode="trilinear",
                      fuse_tv=fuse)
         losses = []
         for i in range(4):
             o, d, tgt = tp.camera_batch(T, 0.691, imgs, R, 120 + i, 2.0)
             losses.append(tr.step_rays(o.to(DEV), d.to(DEV), tgt.to(DEV)).cpu().clone())
-        runs[fuse] = (tr.grid.cpu(), tr.opt.exp_avg.cpu(), tr.opt.exp_avg_sq.cpu(), tr.opt.abs_grad.cpu(),
-                      torch.stack(losses))
-    for a, b in zip(runs[True], runs[False]):
-        assert torch.equal(a, b)
-    assert not torch.equal(runs[True][0], grid0.cpu())
+        runs[fuse] = (tr.grid.cpu(), torch.stack(losses))
+    np.testing.assert_allclose(runs[True][1].numpy(), runs[False][1].numpy(), rtol=1e-5)
+    # Adam turns rounding-level gradient differences on cells with ~0 gradient into
+    # step-size differences (as in the reference-loop test above)
+    diff = (runs[True][0] - runs[False][0]).abs()
+    assert float(diff.max()) <= 5 * 0.0075
+    assert float((diff > 1e-5).float().mean()) < 0.01
