@@ -16,13 +16,19 @@
 
 // Warps of the persistent kernel sit in different phases (gather, scan, scatter) of
 // different rays, so the whole kernel body competes for the instruction cache: the
-// per-sample gather and scatter are kept out of line (one copy each), which measured
-// 1.66x faster than inlining them into every unrolled slot.
+// per-sample gather and scatter must exist once, not once per unrolled slot (unrolled
+// inline copies measured 1.66x slower). PGB_BATCH_LOOP=1 keeps one inline copy of each in
+// a slot loop that is not unrolled, moving each slot's values in and out of the register
+// arrays by compile-time selects; PGB_BATCH_LOOP=0 calls out-of-line functions instead,
+// whose reference arguments and saved registers go through the stack.
+#ifndef PGB_BATCH_LOOP
+#define PGB_BATCH_LOOP 1
+#endif
 #ifndef PGB_SCATTER_INLINE
-#define PGB_SCATTER_INLINE 0
+#define PGB_SCATTER_INLINE PGB_BATCH_LOOP
 #endif
 #ifndef PGB_BATCH_GATHER_INLINE
-#define PGB_BATCH_GATHER_INLINE 0
+#define PGB_BATCH_GATHER_INLINE PGB_BATCH_LOOP
 #endif
 // Resident 256-thread blocks per SM the register allocation must allow.
 #ifndef PGB_BATCH_MIN_BLOCKS
@@ -183,12 +189,29 @@ __global__ void __launch_bounds__(kBatchMaxThreads, PGB_BATCH_MIN_BLOCKS) batch_
     int last = -1;
 
     auto gather = [&](int c) {
+#if PGB_BATCH_LOOP
+#pragma unroll 1
+      for (int k = 0; k < K; ++k) {
+        float t[4], nx, ny, nz;
+        uint32_t b;
+        if (batch_sample<Store, MODE>(ra, ray, sc, (c * K + k) * kWarp + lane, t, b, nx, ny, nz))
+          cs.put(k, lane, nx, ny, nz);
+#pragma unroll
+        for (int kk = 0; kk < K; ++kk) {
+          if (kk == k) {
+            v[kk][0] = t[0]; v[kk][1] = t[1]; v[kk][2] = t[2]; v[kk][3] = t[3];
+            bits[kk] = b;
+          }
+        }
+      }
+#else
 #pragma unroll
       for (int k = 0; k < K; ++k) {
         float nx, ny, nz;
         if (batch_sample<Store, MODE>(ra, ray, sc, (c * K + k) * kWarp + lane, v[k], bits[k], nx, ny, nz))
           cs.put(k, lane, nx, ny, nz);
       }
+#endif
     };
 
     for (int c = 0; c < nchunks; ++c) {
@@ -229,25 +252,39 @@ __global__ void __launch_bounds__(kBatchMaxThreads, PGB_BATCH_MIN_BLOCKS) batch_
         scan_chunk<float, K>(v, __shfl_sync(kFull, Tstart, c), lane, Ts);
       }
       __syncwarp();
+#if PGB_BATCH_LOOP
+#pragma unroll 1
+#else
 #pragma unroll
+#endif
       for (int k = K - 1; k >= 0; --k) {
+        float vk[4], tk;
+        uint32_t bk;
+#pragma unroll
+        for (int kk = 0; kk < K; ++kk) {
+          if (kk == k) {
+            vk[0] = v[kk][0]; vk[1] = v[kk][1]; vk[2] = v[kk][2]; vk[3] = v[kk][3];
+            bk = bits[kk];
+            tk = Ts[kk];
+          }
+        }
         // a slot with alpha 0 and nothing to scatter leaves S unchanged (identity maps)
-        if (PGB_SLOT_SKIP && !__any_sync(kFull, bits[k] != 0u || v[k][3] != 0.f)) continue;
-        const float al = v[k][3];
-        const float G = gpx[0] * v[k][0] + gpx[1] * v[k][1] + gpx[2] * v[k][2] + gpx[3];
+        if (PGB_SLOT_SKIP && !__any_sync(kFull, bk != 0u || vk[3] != 0.f)) continue;
+        const float al = vk[3];
+        const float G = gpx[0] * vk[0] + gpx[1] * vk[1] + gpx[2] * vk[2] + gpx[3];
         float fa = G * al, fb = 1.f - al;
         warp_suffix_affine(fa, fb, lane);
         const float S_here = fa + fb * Snext_carry;
         float S_after = __shfl_down_sync(kFull, S_here, 1);
         if (lane == kWarp - 1) S_after = Snext_carry;
         Snext_carry = __shfl_sync(kFull, S_here, 0);
-        if (bits[k] != 0u) {
-          const float w = al * Ts[k];
-          float dv[4] = {gpx[0] * w, gpx[1] * w, gpx[2] * w, Ts[k] * (G - S_after)};
+        if (bk != 0u) {
+          const float w = al * tk;
+          float dv[4] = {gpx[0] * w, gpx[1] * w, gpx[2] * w, tk * (G - S_after)};
           if (!(dv[0] != 0.f || dv[1] != 0.f || dv[2] != 0.f || dv[3] != 0.f)) continue;
           float nx, ny, nz;
           cs.get(k, lane, nx, ny, nz);
-          sample_scatter<float, MODE>(ra.g, grad, nx, ny, nz, dv, bits[k]);
+          sample_scatter<float, MODE>(ra.g, grad, nx, ny, nz, dv, bk);
         }
       }
     }
