@@ -192,13 +192,13 @@ def torch_gpu_rate(W, grid, T, imgs, dev, steps=3):
                 sample=f"{R} rays x {S} samples, same scene, {steps} steps after 1 warm-up")
 
 
-def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup):
-    """Same workload with the grid stored as `dtype` (fp32 arithmetic and gradients):
-    rays/s of the whole step and the fused kernel's time."""
+def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup, mode=None):
+    """Same workload with the grid stored as `dtype` (fp32 arithmetic and gradients), or
+    with another lookup mode: rays/s of the whole step and the fused kernel's time."""
     S, R = W["samples"], W["rays"]
     g = grid.to(dtype)
-    step = pg.FusedTrainStep(g, 3.0 / W["grid"], S, (W["far"] - W["near"]) / S, mode=W["mode"],
-                             stratified=True, seed=7, overlap_zero=True)
+    step = pg.FusedTrainStep(g, 3.0 / W["grid"], S, (W["far"] - W["near"]) / S,
+                             mode=mode or W["mode"], stratified=True, seed=7, overlap_zero=True)
     stream = torch.cuda.current_stream(dev)
     for i in range(warmup):
         step.step_cameras(T, imgs, W["camera_angle_x"], R, 5000 + i, near=W["near"])
@@ -547,6 +547,12 @@ def main():
     roofline["traffic_vs_random_read_ceiling"] = roofline["traffic_gbs_at_kernel_time"] / rnd["read_sector_gbs"]
     line["bf16_storage"] = storage_leg(pg, grid, T, imgs, W, dev, torch.bfloat16, args.steps,
                                        args.warmup)
+    nearest = storage_leg(pg, grid, T, imgs, W, dev, torch.float32, args.steps, args.warmup,
+                          mode="nearest")
+    nearest.pop("storage")
+    nearest["note"] = ("same workload with nearest-cell lookup (the lookup scripts/train.py "
+                       "trains with); fp32 cells")
+    line["nearest_lookup"] = nearest
     line["full_training_step"] = full_step_leg(pg, grid, T, imgs, W, dev, args.steps, args.warmup)
     if not args.no_batched:
         del step

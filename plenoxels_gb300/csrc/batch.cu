@@ -30,9 +30,10 @@
 #ifndef PGB_BATCH_GATHER_INLINE
 #define PGB_BATCH_GATHER_INLINE PGB_BATCH_LOOP
 #endif
-// Resident 256-thread blocks per SM the register allocation must allow.
+// Resident 256-thread blocks per SM the register allocation must allow. The slot loop
+// needs ~128 registers; capping it at 80 for a third block spills and measured slower.
 #ifndef PGB_BATCH_MIN_BLOCKS
-#define PGB_BATCH_MIN_BLOCKS 3
+#define PGB_BATCH_MIN_BLOCKS 2
 #endif
 // Skip the transmittance and adjoint scans of slots with nothing in them (exact).
 #ifndef PGB_SLOT_SKIP
