@@ -292,7 +292,7 @@ def batched_leg(pg, dev, steps=30, seed=11, num_scenes=64):
     R = sum(o.shape[0] for o in origins)
     step = BatchedTrainStep(scs, R, term_threshold=1e-4)
     step.set_rays(torch.cat(origins), torch.cat(dirs), torch.cat(targets), torch.cat(owners))
-    tiles = step.autotune(reps=3)
+    tiles = step.autotune(reps=3, brick_sizes=(0, 1, 2))
     step.capture()
     for _ in range(3):
         step.step()
@@ -312,6 +312,7 @@ def batched_leg(pg, dev, steps=30, seed=11, num_scenes=64):
             "scenes": len(scs), "cells": cells, "occupied_cells": occ_cells, "samples": S,
             "p50_ms": p50, "p99_ms": p99, "tiles": {f"K{k}_t{t}": v for (k, t), v in tiles.items()},
             "chosen_tile": f"K{step.tiles[0]}_t{step.tiles[1]}",
+            "chosen_brick_cells": 1 << step.brick_log2,
             "note": "BF16 cells, occupancy-masked fp32 gradients, early termination at T<1e-4, "
                     "CUDA-graph replay of zeroing + one persistent launch; same rays every step"}
 

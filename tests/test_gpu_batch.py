@@ -107,6 +107,16 @@ def test_skipping_is_exact_and_termination_is_bounded():
     for x, y, sc in zip(ga, [s.grad for s in b.scenes], a.scenes):
         m = sc.occupancy.unsqueeze(-1)
         assert float(((x - y) * m).abs().max()) <= 1e-6 * float((y * m).abs().max()) + 1e-12
+    # every brick size skips exactly (down to single cells)
+    for L in (0, 1, 2, 4):
+        e, _ = _batch(problem, term_threshold=0.0)
+        e._set_bricks(L)
+        e.step()
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(ra.cpu().numpy(), e.rgba.cpu().numpy(), rtol=1e-6, atol=1e-7)
+        for x, sc in zip(ga, e.scenes):
+            m = sc.occupancy.unsqueeze(-1)
+            assert float(((x - sc.grad) * m).abs().max()) <= 1e-6 * float((x * m).abs().max()) + 1e-12
     # early termination: only contributions behind T < 1e-4 may change
     c, _ = _batch(problem, term_threshold=1e-4)
     c.step()
@@ -117,8 +127,8 @@ def test_skipping_is_exact_and_termination_is_bounded():
 def test_graph_replay_on_new_rays_and_autotune():
     problem = _make(torch.bfloat16, seed=3)
     step, R = _batch(problem, term_threshold=1e-4)
-    times = step.autotune(reps=2)
-    assert step.tiles in times and len(times) >= 3
+    times = step.autotune(reps=2, brick_sizes=(1, 2, 3))
+    assert step.tiles in times and len(times) >= 3 and step.brick_log2 in (1, 2, 3)
     eager = float(step.step())
     torch.cuda.synchronize()
     g_eager = [sc.grad.clone() for sc in step.scenes]
