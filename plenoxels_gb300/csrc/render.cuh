@@ -411,6 +411,9 @@ __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ra
 #ifndef PGB_SLOT_SKIP
 #define PGB_SLOT_SKIP 0  // 1: skip the scans of slots whose 32 samples all have alpha 0
 #endif                   //    (exact; a vote per slot costs more than it saves here)
+#ifndef PGB_REVERSE_LOOP
+#define PGB_REVERSE_LOOP 0  // 1: one copy of the reverse-pass body in a slot loop
+#endif
 #ifndef PGB_SKIP_ZERO_DV
 #define PGB_SKIP_ZERO_DV 1  // skip the scatter of samples whose four partials are all 0
 #endif
@@ -604,25 +607,39 @@ render_kernel(const RenderArgs<Real> a) {
         }
       }
       __syncwarp();
+#if PGB_REVERSE_LOOP
+#pragma unroll 1
+#else
 #pragma unroll
+#endif
       for (int k = K - 1; k >= 0; --k) {
+        Real vk[4], tk;
+        uint32_t bk;
+#pragma unroll
+        for (int kk = 0; kk < K; ++kk) {
+          if (kk == k) {
+            vk[0] = v[kk][0]; vk[1] = v[kk][1]; vk[2] = v[kk][2]; vk[3] = v[kk][3];
+            bk = bits[kk];
+            tk = Ts[kk];
+          }
+        }
         // a slot with alpha 0 and nothing to scatter leaves S unchanged (identity maps)
-        if (PGB_SLOT_SKIP && !__any_sync(kFull, bits[k] != 0u || v[k][3] != Real(0))) continue;
-        const Real al = v[k][3];
-        const Real G = gpx[0] * v[k][0] + gpx[1] * v[k][1] + gpx[2] * v[k][2] + gpx[3];
+        if (PGB_SLOT_SKIP && !__any_sync(kFull, bk != 0u || vk[3] != Real(0))) continue;
+        const Real al = vk[3];
+        const Real G = gpx[0] * vk[0] + gpx[1] * vk[1] + gpx[2] * vk[2] + gpx[3];
         Real fa = G * al, fb = Real(1) - al;
         warp_suffix_affine(fa, fb, lane);
         const Real S_here = fa + fb * Snext_carry;          // S_s for this lane's sample
         Real S_after = __shfl_down_sync(kFull, S_here, 1);  // S_{s+1}
         if (lane == kWarp - 1) S_after = Snext_carry;
         Snext_carry = __shfl_sync(kFull, S_here, 0);
-        if (bits[k] != 0u) {
-          const Real w = al * Ts[k];
+        if (bk != 0u) {
+          const Real w = al * tk;
           Real dv[4];
           dv[0] = gpx[0] * w;
           dv[1] = gpx[1] * w;
           dv[2] = gpx[2] * w;
-          dv[3] = Ts[k] * (G - S_after);
+          dv[3] = tk * (G - S_after);
           if (with_beta) {
             const Real e = (Real)a.beta_eps;
             dv[3] += (Real)(a.beta_w * a.inv_samples) * (Real(1) / (al + e) + Real(1) / (Real(1) - al + e));
@@ -637,7 +654,7 @@ render_kernel(const RenderArgs<Real> a) {
           } else {
             sample_coords(a, ray, (c * K + k) * kWarp + lane, nx, ny, nz);
           }
-          sample_scatter<Real, MODE>(a.g, a.grad, nx, ny, nz, dv, bits[k]);
+          sample_scatter<Real, MODE>(a.g, a.grad, nx, ny, nz, dv, bk);
         }
       }
     }
