@@ -412,8 +412,8 @@ __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ra
 #define PGB_SLOT_SKIP 0  // 1: skip the scans of slots whose 32 samples all have alpha 0
 #endif                   //    (exact; a vote per slot costs more than it saves here)
 #ifndef PGB_REVERSE_LOOP
-#define PGB_REVERSE_LOOP 0  // 1: one copy of the reverse-pass body in a slot loop
-#endif
+#define PGB_REVERSE_LOOP 1  // one copy of the reverse-pass body in a slot loop (the gather
+#endif                      // stays unrolled for its load parallelism): 0.158 -> 0.147 ms
 #ifndef PGB_SKIP_ZERO_DV
 #define PGB_SKIP_ZERO_DV 1  // skip the scatter of samples whose four partials are all 0
 #endif
