@@ -337,9 +337,6 @@ PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, 
 #ifndef PGB_RENDER_MIN_BLOCKS
 #define PGB_RENDER_MIN_BLOCKS 0
 #endif
-#ifndef PGB_GATHER_UNROLL
-#define PGB_GATHER_UNROLL 0  // 0: fully unrolled slot loop
-#endif
 #ifndef PGB_COORDS_IN_SMEM
 #define PGB_COORDS_IN_SMEM 1
 #endif
@@ -389,11 +386,7 @@ template <typename Real, typename Store, int MODE, int K, bool ADJ>
 __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ray<Real>& ray, int c,
                                              int lane, Real v[K][4], uint32_t bits[K],
                                              CoordStage<Real, K>& cs) {
-#if PGB_GATHER_UNROLL == 0
 #pragma unroll
-#else
-#pragma unroll PGB_GATHER_UNROLL
-#endif
   for (int k = 0; k < K; ++k) {
     const int s = (c * K + k) * kWarp + lane;
     v[k][0] = v[k][1] = v[k][2] = v[k][3] = Real(0);
