@@ -405,8 +405,9 @@ __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ra
 #define PGB_SLOT_SKIP 0  // 1: skip the scans of slots whose 32 samples all have alpha 0
 #endif                   //    (exact; a vote per slot costs more than it saves here)
 #ifndef PGB_REVERSE_LOOP
-#define PGB_REVERSE_LOOP 1  // one copy of the reverse-pass body in a slot loop (the gather
-#endif                      // stays unrolled for its load parallelism): 0.158 -> 0.147 ms
+#define PGB_REVERSE_LOOP 1  // 1: one copy of the trilinear reverse-pass body in a slot loop
+#endif                      // (the gather stays unrolled for its load parallelism):
+                            // 0.158 -> 0.147 ms; 2: also for nearest; 0: unrolled
 #ifndef PGB_SKIP_ZERO_DV
 #define PGB_SKIP_ZERO_DV 1  // skip the scatter of samples whose four partials are all 0
 #endif
@@ -600,11 +601,10 @@ render_kernel(const RenderArgs<Real> a) {
         }
       }
       __syncwarp();
-#if PGB_REVERSE_LOOP
-#pragma unroll 1
-#else
-#pragma unroll
-#endif
+      // trilinear: a loop (the 8-corner scatter body is large); nearest: unrolled
+      constexpr int kRevUnroll =
+          (PGB_REVERSE_LOOP == 2 || (PGB_REVERSE_LOOP == 1 && MODE == PGB_TRILINEAR)) ? 1 : K;
+#pragma unroll kRevUnroll
       for (int k = K - 1; k >= 0; --k) {
         Real vk[4], tk;
         uint32_t bk;
