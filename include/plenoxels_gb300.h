@@ -187,8 +187,10 @@ int pgb_batch_zero_grads(const pgb_scene* scenes, int32_t num_scenes, int64_t ma
  * num_scenes (<= 256) descriptors. Gradients accumulate into each scene's grad_cells;
  * loss_out[0] = loss_weight * mean over all rays and channels of the squared error.
  * term_threshold > 0 stops a ray once its transmittance falls below it (checked every
- * 32*slots_per_lane samples). slots_per_lane in {2,4,8} and threads_per_block in
- * {128,256} are the tile choices (0: defaults). workspace: pgb_batch_workspace_bytes(R),
+ * 32*slots_per_lane samples). slots_per_lane in {1,2,4,8} and threads_per_block in
+ * {128,256} are the tile choices (0: defaults); a ray spans at most 32 chunks, so every
+ * scene needs num_samples <= 1024 * slots_per_lane (a longer ray's loss and RGBA come
+ * back NaN). workspace: pgb_batch_workspace_bytes(R),
  * zeroed once before first use; the kernel leaves its counters zeroed. */
 int64_t pgb_batch_workspace_bytes(int64_t num_rays);
 int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, int32_t mode,

@@ -80,7 +80,7 @@ class Scene:
         return desc
 
 
-TILE_CANDIDATES = [(2, 256), (2, 128), (4, 256), (4, 128), (8, 256)]
+TILE_CANDIDATES = [(1, 256), (2, 256), (2, 128), (4, 256), (4, 128), (8, 256)]
 
 
 class BatchedTrainStep:
@@ -91,7 +91,7 @@ class BatchedTrainStep:
     buffers (capacity max_rays), so a captured graph replays on new rays."""
 
     def __init__(self, scenes, max_rays, mode="trilinear", clip=True, term_threshold=1e-4,
-                 stratified=False, seed=0, loss_weight=1.0, tiles=(2, 256), brick_log2=BRICK_LOG2):
+                 stratified=False, seed=0, loss_weight=1.0, tiles=None, brick_log2=BRICK_LOG2):
         if not scenes:
             raise ValueError("a batch needs at least one scene")
         dtypes = {sc.cells.dtype for sc in scenes}
@@ -105,12 +105,16 @@ class BatchedTrainStep:
         self.stratified = bool(stratified)
         self.seed = int(seed)
         self.loss_weight = float(loss_weight)
+        self.max_samples = max(int(sc.num_samples) for sc in scenes)
+        if tiles is None:
+            tiles = (next((k for k in (2, 4, 8) if 32 * 32 * k >= self.max_samples), 8), 256)
         self.tiles = tuple(tiles)
         dev = scenes[0].cells.device
         self.device = dev
-        for sc in scenes:
-            if sc.num_samples > 32 * 32 * 2:
-                raise NotImplementedError("at most 2048 samples per ray in the batched form")
+        if self.max_samples > 32 * 32 * 8:
+            raise NotImplementedError("at most 8192 samples per ray in the batched form")
+        if not self._tile_fits(self.tiles):
+            raise ValueError(f"tile {self.tiles} cannot cover {self.max_samples} samples per ray")
         self.brick_log2 = None
         self._set_bricks(brick_log2)
         self.max_cells = max(int(sc.cells.shape[0] * sc.cells.shape[1] * sc.cells.shape[2]) for sc in scenes)
@@ -126,6 +130,10 @@ class BatchedTrainStep:
         self.loss = torch.zeros((), device=dev)
         self.rgba = None
         self.graph = None
+
+    def _tile_fits(self, tile):
+        # a ray spans at most 32 chunks of 32 * K samples
+        return 32 * 32 * int(tile[0]) >= self.max_samples
 
     def _set_bricks(self, brick_log2):
         """(Re)builds every scene's dilated brick mask at 2^brick_log2 cells a side and the
@@ -195,7 +203,7 @@ class BatchedTrainStep:
         for L in (brick_sizes or (self.brick_log2,)):
             self._set_bricks(L)
             times = {}
-            for tile in candidates:
+            for tile in (t for t in candidates if self._tile_fits(t)):
                 self._run(tile)
                 torch.cuda.synchronize(self.device)
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -182,6 +182,11 @@ __global__ void __launch_bounds__(kBatchMaxThreads, PGB_BATCH_MIN_BLOCKS) batch_
     ray.h = a.stratified ? hash_stream(a.seed, (uint64_t)r) : 0ull;
 
     const int nchunks = (ra.S + kWarp * K - 1) / (kWarp * K);
+    if (nchunks > kWarp) {  // a chunk start per lane: more chunks are not supported
+      if (lane == 0) a.ray_loss[r] = __longlong_as_double(0x7ff8000000000000ll);  // NaN loss
+      if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = __int_as_float(0x7fc00000);
+      continue;
+    }
     float v[K][4];
     uint32_t bits[K];
     float Ts[K];
@@ -424,6 +429,7 @@ int launch_batch_k(const BatchArgs& a, int threads, cudaStream_t s) {
 template <typename Store, int MODE>
 int launch_batch_m(const BatchArgs& a, int K, int threads, cudaStream_t s) {
   switch (K) {
+    case 1: return launch_batch_k<Store, MODE, 1>(a, threads, s);
     case 2: return launch_batch_k<Store, MODE, 2>(a, threads, s);
     case 4: return launch_batch_k<Store, MODE, 4>(a, threads, s);
     case 8: return launch_batch_k<Store, MODE, 8>(a, threads, s);
@@ -456,7 +462,7 @@ int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, 
   if (((uintptr_t)workspace % 16) != 0) return PGB_ERR_ALIGN;
   const int K = slots_per_lane == 0 ? 2 : slots_per_lane;
   const int threads = threads_per_block == 0 ? 256 : threads_per_block;
-  if (K != 2 && K != 4 && K != 8) return PGB_ERR_ARG;
+  if (K != 1 && K != 2 && K != 4 && K != 8) return PGB_ERR_ARG;
   if (threads != 128 && threads != 256) return PGB_ERR_ARG;
   BatchArgs a = {};
   a.scenes = scenes;

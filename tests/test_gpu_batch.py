@@ -158,3 +158,42 @@ def test_invalid_scene_index_contributes_nothing():
     step.step()
     torch.cuda.synchronize()
     assert float(step.rgba[:10].abs().sum()) == 0.0
+
+
+@pytest.mark.parametrize("tiles", [(1, 256), (4, 128)])
+def test_every_tile_gives_the_oracle_step(tiles):
+    """A 32-sample chunk per ray (K = 1) and a 128-sample one (K = 4) on the same batch."""
+    problem = _make(torch.float32, seed=11)
+    step, R = _batch(problem, term_threshold=0.0, tiles=tiles)
+    loss = float(step.step())
+    torch.cuda.synchronize()
+    rgba_ref, grads, loss_ref = _oracle(problem, R)
+    np.testing.assert_allclose(step.rgba.cpu().numpy(), rgba_ref.numpy(), rtol=1e-5, atol=2e-6)
+    np.testing.assert_allclose(loss, loss_ref, rtol=1e-5)
+    assert _grad_err(step, grads) < 1e-4
+
+
+def test_long_rays_take_a_tile_that_covers_them():
+    """2500 samples per ray need 32 * 32 * K >= 2500: the default tile is K = 4, a K = 2 tile
+    is refused on the host, and the autotuner only tries tiles that fit."""
+    side, rays, S = 12, 40, 2500
+    g = torch.from_numpy(scenes.make_grid(side, 2, 77, amp=(0.05, 0.3)))
+    occ = g[..., 3] > torch.quantile(g[..., 3].flatten(), 0.7)
+    g[~occ] = 0.0
+    T = torch.from_numpy(scenes.make_cameras(2, 78))
+    imgs = torch.from_numpy(scenes.make_images(2, 8, 8, 79))
+    o, d, tgt = tp.camera_batch(T, 0.691, imgs, rays, 80, 2.0)
+    problem = [dict(cells=g, occ=occ, o=o, d=d, tgt=tgt, S=S, side=side,
+                    pd=scenes.points_distance(side), delta=4.0 / S)]
+    with pytest.raises(ValueError):
+        _batch(problem, term_threshold=0.0, tiles=(2, 256))
+    step, R = _batch(problem, term_threshold=0.0)
+    assert step.tiles[0] == 4
+    times = step.autotune(reps=1)
+    assert all(32 * 32 * k >= S for k, _ in times)
+    loss = float(step.step())
+    torch.cuda.synchronize()
+    rgba_ref, grads, loss_ref = _oracle(problem, R)
+    np.testing.assert_allclose(step.rgba.cpu().numpy(), rgba_ref.numpy(), rtol=1e-5, atol=2e-6)
+    np.testing.assert_allclose(loss, loss_ref, rtol=1e-5)
+    assert _grad_err(step, grads) < 1e-4
