@@ -31,6 +31,9 @@ int launch_render_logt_bf16(const RenderArgs<float>& a, int mode, int phase, cud
 // Slots per lane (K) used for a ray of S samples: one chunk up to 512 samples,
 // 256-sample chunks beyond.
 inline int pick_slots(int S) {
+#ifdef PGB_FORCE_SLOTS
+  if (S <= 32 * kMaxChunks * PGB_FORCE_SLOTS) return PGB_FORCE_SLOTS;
+#endif
   if (S <= 64) return 2;
   if (S <= 128) return 4;
   if (S <= 256) return 8;
