@@ -39,6 +39,12 @@ def grid_min(shape, points_distance: float, dtype=torch.float32):
 
 
 # ----------------------------------------------------------------------- rays
+def _plain_norm3(v):
+    """sqrt((x*x + y*y) + z*z) over the last dim of [N,3], each op rounded separately."""
+    x, y, z = v[..., 0], v[..., 1], v[..., 2]
+    return ((x * x + y * y) + z * z).sqrt()
+
+
 def camera_rays(transforms, camera_angle_x, imgs, uv):
     """Directions and target pixels of camera rays from uniforms uv [C,R,2].
     src/ray_sampling.py:212-264 (generate_rays_batched), same op order."""
@@ -46,7 +52,10 @@ def camera_rays(transforms, camera_angle_x, imgs, uv):
     x_axis = transforms[:, :3, 0]
     y_axis = transforms[:, :3, 1]
     z_axis = -transforms[:, :3, 2]
-    aspect = x_axis.norm(dim=1) / y_axis.norm(dim=1)
+    # torch's norm over these strided views rounds every op on x86 (where the golden
+    # fixtures were made from the reference) but contracts to FMAs on aarch64; the
+    # explicit form below is the x86 rounding on every platform
+    aspect = _plain_norm3(x_axis) / _plain_norm3(y_axis)
     ray = uv.clone()
     pix = uv.clone()
     ray[:, :, 0] = camera_angle_x * (ray[:, :, 0] - 0.5)
