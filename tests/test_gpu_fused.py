@@ -323,3 +323,35 @@ def test_rays_that_miss_the_grid():
     assert float(step.grad.abs().sum()) == 0.0
     px = pg.render_rays(grid, o, d, 0.05, 128, 0.2)
     assert float(px.abs().sum()) == 0.0
+
+
+@pytest.mark.parametrize("mode", ["nearest", "trilinear"])
+def test_rays_clipped_to_the_grid_match_oracle(mode):
+    """Chunks whose samples all lie outside the grid are skipped: axis-parallel rays
+    (zero direction components) inside and outside the box's slabs, rays starting inside
+    the grid, rays pointing away from it, grazing rays along a face, and long rays that
+    cross the box in a few of many chunks must give the oracle's results."""
+    g = torch.Generator().manual_seed(61)
+    side = 24
+    grid = torch.rand(side, side, side, 4, generator=g)
+    grid[..., 3] *= 0.15
+    pd = scenes.points_distance(side)
+    gmin = tp.grid_min(grid.shape, pd)
+    lo = float(gmin[0])
+    hi = lo + side * pd
+    rays = [
+        ([-3.0, 0.1, 0.2], [1.0, 0.0, 0.0]),      # x-parallel through the box
+        ([-3.0, 2.0, 0.2], [1.0, 0.0, 0.0]),      # x-parallel, outside the y slab
+        ([0.1, 0.2, 0.3], [0.0, 1.0, 0.0]),       # starts inside
+        ([0.1, -0.2, 0.3], [0.3, 0.4, 0.866]),    # starts inside, oblique
+        ([3.0, 3.0, 3.0], [0.577, 0.577, 0.577]), # points away
+        ([-3.0, lo, 0.0], [1.0, 0.0, 0.0]),       # along the lower y face
+        ([-3.0, hi, 0.0], [1.0, 0.0, 0.0]),       # along the upper y face (outside)
+        ([-3.0, 0.0, hi - 0.5 * pd], [1.0, 0.0, 0.0]),  # inside the last z cell
+        ([0.0, 0.0, -9.0], [0.0, 0.0, 1.0]),      # long way to the box
+    ]
+    o = torch.tensor([r[0] for r in rays], dtype=torch.float32)
+    d = torch.nn.functional.normalize(torch.tensor([r[1] for r in rays], dtype=torch.float32), dim=1)
+    target = torch.rand(o.shape[0], 4, generator=g)
+    _parity(grid, o, d, target, 1200, 12.0 / 1200, pd, gmin, mode, strat=True)
+    _parity(grid, o, d, target, 96, 0.06, pd, gmin, mode)
