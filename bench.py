@@ -499,24 +499,49 @@ def main():
         cam_pos = torch.repeat_interleave(T[:, :3, 3], R // W["cameras"] + 1, 0)
         o = cam_pos + W["near"] * dirs
         host.append(tuple(x[:n].cpu().pin_memory() for x in (o, dirs, pixels)))
-    dev_o = torch.empty(R, 3, device=dev)
-    dev_d = torch.empty(R, 3, device=dev)
-    dev_t = torch.empty(R, 4, device=dev)
-    loss_host = torch.empty(args.steps, dtype=torch.float32).pin_memory()
+    # two device input buffers: step i+1's batch is copied on a copy stream while step i
+    # runs, as a training loop would pipeline it; every copy is inside the timed region
+    bufs = [tuple(torch.empty(R, c, device=dev) for c in (3, 3, 4)) for _ in range(2)]
+    copy_stream = torch.cuda.Stream(device=dev)
+    loss_host = torch.empty(args.steps + args.warmup, dtype=torch.float32).pin_memory()
     h2d = sum(x.numel() * x.element_size() for x in host[0])
+    free = [None, None]  # event: the step that last read buffer b has run
+
+    def pipelined(i, first_wait=None):
+        b = i % 2
+        with torch.cuda.stream(copy_stream):
+            if first_wait is not None:
+                copy_stream.wait_event(first_wait)
+            if free[b] is not None:
+                copy_stream.wait_event(free[b])
+            for dst, src in zip(bufs[b], host[i % nb]):
+                dst.copy_(src, non_blocking=True)
+            copied = torch.cuda.Event()
+            copied.record(copy_stream)
+        return b, copied
+
+    def run(i, b, copied):
+        stream.wait_event(copied)
+        loss = step.step_rays(*bufs[b])
+        allreduce_gradient(step.grad)
+        loss_host[i].copy_(loss, non_blocking=True)
+        done = torch.cuda.Event()
+        done.record(stream)
+        free[b] = done
+
+    nxt = pipelined(0)
     for i in range(args.warmup):
-        ho, hd, ht = host[i % nb]
-        dev_o.copy_(ho, non_blocking=True); dev_d.copy_(hd, non_blocking=True); dev_t.copy_(ht, non_blocking=True)
-        step.step_rays(dev_o, dev_d, dev_t)
+        cur, nxt = nxt, pipelined(i + 1)
+        run(i, *cur)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for i in range(args.steps):
-        ho, hd, ht = host[i % nb]
-        dev_o.copy_(ho, non_blocking=True); dev_d.copy_(hd, non_blocking=True); dev_t.copy_(ht, non_blocking=True)
-        loss = step.step_rays(dev_o, dev_d, dev_t)
-        allreduce_gradient(step.grad)
-        loss_host[i].copy_(loss, non_blocking=True)
+    nxt = pipelined(args.warmup, first_wait=e0)
+    for i in range(args.warmup, args.warmup + args.steps):
+        cur = nxt
+        if i + 1 < args.warmup + args.steps:
+            nxt = pipelined(i + 1)
+        run(i, *cur)
     e1.record(stream)
     torch.cuda.synchronize(dev)
     e2e_ms = e0.elapsed_time(e1) / args.steps
