@@ -217,6 +217,49 @@ def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup, mode=None):
             "and gradients, cells stored in this type"}
 
 
+def drop_in_leg(pg, grid, T, imgs, W, dev, steps, warmup):
+    """scripts/train.py:129-156 with the reference's imports swapped for this package's
+    drop-in functions: the unfused path, one kernel per reference function (ray
+    generation, sample points, normalisation, nearest lookup with the clip fused, masked
+    compositing, torch's MSE, autograd backward through the hand-written scatters). Same
+    cameras and grid, 82 rays per camera x 100 cameras, 256 samples, nearest lookup (the
+    lookup train.py uses)."""
+    S = W["samples"]
+    per_cam = W["rays"] // W["cameras"]
+    pd = 3.0 / W["grid"]
+    delta = (W["far"] - W["near"]) / S
+    grid_indices, _, _, _ = pg.generate_grid(W["grid"], W["grid"], W["grid"], pd, device=dev)
+    g = grid.clone().requires_grad_(True)
+    stream = torch.cuda.current_stream(dev)
+
+    def one():
+        g.grad = None
+        samples, target, _, _ = pg.sample_camera_rays_batched(T, W["camera_angle_x"], imgs, per_cam, S,
+                                                              delta, False, False, device=dev)
+        n = pg.normalize_samples_for_indecies(grid_indices, samples, pd)
+        vals, mask = pg.get_nearest_voxels(n, g, clip=True)
+        vals = vals * mask.unsqueeze(-1)
+        px = pg.compute_alpha_weighted_pixels(vals.reshape(T.shape[0], per_cam, S, 4))
+        loss = torch.nn.functional.mse_loss(px.reshape(-1, 4), target)
+        loss.backward()
+        return loss
+
+    for _ in range(warmup):
+        one()
+    torch.cuda.synchronize(dev)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        one()
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = t0.elapsed_time(t1) / steps
+    rays = per_cam * W["cameras"]
+    return {"value": rays / (ms / 1e3), "unit": "rays/s", "ms_per_step": ms, "rays": rays,
+            "note": "the reference's train.py step composed from the drop-in functions "
+                    "(import swap only), nearest lookup, torch.rand ray draws, autograd"}
+
+
 def random_access_ceiling(pg, dev, reads=1 << 24, reps=5):
     """The GPU's rate for independent random 32 B sectors out of a 256 MiB buffer (16 B
     loads, and float4 atomic adds), each launch after a 256 MiB write that evicts L2:
@@ -596,6 +639,7 @@ def main():
     nearest["note"] = ("same workload with nearest-cell lookup (the lookup scripts/train.py "
                        "trains with); fp32 cells")
     line["nearest_lookup"] = nearest
+    line["drop_in_path"] = drop_in_leg(pg, grid, T, imgs, W, dev, args.steps, args.warmup)
     line["full_training_step"] = full_step_leg(pg, grid, T, imgs, W, dev, args.steps, args.warmup)
     if not args.no_batched:
         del step
