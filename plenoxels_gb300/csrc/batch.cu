@@ -30,8 +30,13 @@
 #ifndef PGB_BATCH_GATHER_INLINE
 #define PGB_BATCH_GATHER_INLINE PGB_BATCH_LOOP
 #endif
-// Resident 256-thread blocks per SM the register allocation must allow. The slot loop
-// needs ~128 registers; capping it at 80 for a third block spills and measured slower.
+// Resident 256-thread blocks per SM the register allocation must allow. With 32-sample
+// chunks (K = 1) a cap of 80 registers for a third block spills a little and measured
+// faster (64-scene step 7.32 -> 6.78 ms); longer chunks keep two blocks (their spills
+// at 80 registers cost more than the extra warps give).
+#ifndef PGB_BATCH_MIN_BLOCKS_K1
+#define PGB_BATCH_MIN_BLOCKS_K1 3
+#endif
 #ifndef PGB_BATCH_MIN_BLOCKS
 #define PGB_BATCH_MIN_BLOCKS 2
 #endif
@@ -130,7 +135,8 @@ PGB_BATCH_GATHER_ATTR bool batch_sample(const RenderArgs<float>& ra, const Ray<f
 }
 
 template <typename Store, int MODE, int K>
-__global__ void __launch_bounds__(kBatchMaxThreads, PGB_BATCH_MIN_BLOCKS) batch_train_kernel(const BatchArgs a) {
+__global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCKS_K1 : PGB_BATCH_MIN_BLOCKS)
+    batch_train_kernel(const BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   pgb_scene* sc_tab = reinterpret_cast<pgb_scene*>(smem_raw);
   const size_t tab_bytes = ((size_t)a.num_scenes * sizeof(pgb_scene) + 15) & ~(size_t)15;
