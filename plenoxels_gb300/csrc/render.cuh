@@ -337,6 +337,9 @@ PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, 
 #ifndef PGB_RENDER_MIN_BLOCKS
 #define PGB_RENDER_MIN_BLOCKS 0
 #endif
+#ifndef PGB_RENDER_MIN_BLOCKS_NEAREST
+#define PGB_RENDER_MIN_BLOCKS_NEAREST PGB_RENDER_MIN_BLOCKS
+#endif
 #ifndef PGB_COORDS_IN_SMEM
 #define PGB_COORDS_IN_SMEM 1
 #endif
@@ -488,7 +491,8 @@ constexpr int render_smem_bytes(int warps_per_block) {
 // LOGT: transmittance as the compensated log-sum (scan_chunk_log, fp32 only) instead of
 // the reference's product scan.
 template <typename Real, typename Store, int MODE, int K, int PHASE, bool LOGT = false>
-__global__ void __launch_bounds__(kRenderThreads, PGB_RENDER_MIN_BLOCKS)
+__global__ void __launch_bounds__(kRenderThreads, MODE == PGB_NEAREST ? PGB_RENDER_MIN_BLOCKS_NEAREST
+                                                                      : PGB_RENDER_MIN_BLOCKS)
 render_kernel(const RenderArgs<Real> a) {
   static_assert(!LOGT || sizeof(Real) == 4, "log-sum transmittance is an fp32 form");
   extern __shared__ __align__(16) unsigned char smem_raw[];
