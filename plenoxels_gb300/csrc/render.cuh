@@ -337,8 +337,10 @@ PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, 
 #ifndef PGB_RENDER_MIN_BLOCKS
 #define PGB_RENDER_MIN_BLOCKS 0
 #endif
+// Nearest lookup (one load per sample) gains from more resident warps even at 64
+// registers with spills: 4 blocks per SM measured 0.0697 ms against 0.0765 ms at 2.
 #ifndef PGB_RENDER_MIN_BLOCKS_NEAREST
-#define PGB_RENDER_MIN_BLOCKS_NEAREST PGB_RENDER_MIN_BLOCKS
+#define PGB_RENDER_MIN_BLOCKS_NEAREST 4
 #endif
 #ifndef PGB_COORDS_IN_SMEM
 #define PGB_COORDS_IN_SMEM 1
