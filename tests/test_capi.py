@@ -106,6 +106,17 @@ def test_argument_validation_without_launch(lib):
     r.num_samples = 10 ** 6
     assert lib.pgb_render_fwd(ctypes.byref(g), ctypes.byref(r), 16, None) == _lib.PGB_ERR_UNSUPPORTED
     r.num_samples = 8
+    # the log-sum transmittance needs clipped fp32/BF16 cells
+    r.log_transmittance = 1
+    g.clip = 0
+    assert lib.pgb_render_fwd(ctypes.byref(g), ctypes.byref(r), 16, None) == _lib.PGB_ERR_ARG
+    g.clip = 1
+    g.dtype = _lib.PGB_F64
+    g.cells = 512
+    assert lib.pgb_render_fwd(ctypes.byref(g), ctypes.byref(r), 16, None) == _lib.PGB_ERR_UNSUPPORTED
+    g.dtype = _lib.PGB_F32
+    g.cells = 256
+    r.log_transmittance = 0
     assert lib.pgb_render_fwd(ctypes.byref(g), ctypes.byref(r), 16, None) == _lib.PGB_ERR_ARG  # no rays
     assert lib.pgb_render_train(ctypes.byref(g), ctypes.byref(r), None, 1.0, None, None, None, None,
                                 None) == _lib.PGB_ERR_ARG
