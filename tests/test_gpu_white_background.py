@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 DEV = "cuda"
 
 
-def _config0():
+def _scene_64cube():
     side, res, S, near, far = 64, 64, 128, 2.0, 6.0
     grid = torch.from_numpy(scenes.make_grid(side, 3, 1000))
     truth = torch.from_numpy(scenes.make_grid(side, 3, 2000))
@@ -34,8 +34,8 @@ def _config0():
 
 
 @pytest.mark.parametrize("background", [True, False])
-def test_config0_step_matches_oracle(background):
-    grid, o, d, target, S, delta, pd, gmin, white = _config0()
+def test_white_background_step_matches_oracle(background):
+    grid, o, d, target, S, delta, pd, gmin, white = _scene_64cube()
     bg = white if background else None
     g = grid.clone().requires_grad_(True)
     px_ref = tp.render(g, o, d, S, delta, gmin, pd, "nearest", background=bg)
