@@ -508,6 +508,8 @@ render_kernel(const RenderArgs<Real> a) {
   double loss_lane = 0.0;
   double beta_lane = 0.0;
   const bool with_beta = PHASE == kTrain && a.beta_w != 0.0;
+  // beta_w / (R*S) * (1 + 2 eps): the numerator of 1/(alpha+eps) + 1/(1-alpha+eps)
+  const Real beta_scale = (Real)(a.beta_w * a.inv_samples * (1.0 + 2.0 * (double)a.beta_eps));
   __shared__ double s_part[32];  // per-warp loss partials (training phase)
   __shared__ double s_part_beta[32];
   __shared__ unsigned s_done;    // warps of this block that finished (training phase)
@@ -550,14 +552,16 @@ render_kernel(const RenderArgs<Real> a) {
         acc[2] += w * v[k][2];
         acc[3] += w;
       }
-      if (with_beta) {
+      if (with_beta) {  // per-chunk partial in Real, one fp64 add per chunk
+        Real bsum = Real(0);
 #pragma unroll
         for (int k = 0; k < K; ++k) {
           if ((c * K + k) * kWarp + lane < a.S) {
             const Real al = v[k][3], e = (Real)a.beta_eps;
-            beta_lane += (double)(log(al + e) - log(Real(1) - al + e));
+            bsum += log(al + e) - log(Real(1) - al + e);
           }
         }
+        beta_lane += (double)bsum;
       }
       last = c;
       if (a.term_thr > 0.0f && T < (Real)a.term_thr) break;
@@ -639,9 +643,9 @@ render_kernel(const RenderArgs<Real> a) {
           dv[1] = gpx[1] * w;
           dv[2] = gpx[2] * w;
           dv[3] = tk * (G - S_after);
-          if (with_beta) {
+          if (with_beta) {  // d/dalpha of log(alpha + e) - log(1 - alpha + e), one division
             const Real e = (Real)a.beta_eps;
-            dv[3] += (Real)(a.beta_w * a.inv_samples) * (Real(1) / (al + e) + Real(1) / (Real(1) - al + e));
+            dv[3] += beta_scale / ((al + e) * (Real(1) - al + e));
           }
           // behind an opaque sample (T = 0) every partial is 0 and no corner would be written
           if (PGB_SKIP_ZERO_DV &&
