@@ -173,16 +173,19 @@ typedef struct {
 int pgb_build_bricks(const uint32_t* cell_bits, const int32_t dims[3], int32_t brick_log2,
                      uint32_t* bricks_out, pgb_stream_t stream);
 
-/* Packs a uint8/bool mask of count entries into bits (bit c of word c/32). */
+/* Packs a uint8/bool mask of count entries into bits (bit c of word c/32). No counterpart
+ * in the reference (batched form). */
 int pgb_pack_mask(const uint8_t* mask, int64_t count, uint32_t* bits_out, pgb_stream_t stream);
 
-/* Zeroes the gradients of all scenes of a device-resident scene table: the occupied
+/* No counterpart in the reference (batched form). Zeroes the gradients of all scenes of
+ * a device-resident scene table: the occupied
  * cells where a scene has an occupancy mask (the only cells the step writes), every cell
  * otherwise. max_cells bounds the largest scene. */
 int pgb_batch_zero_grads(const pgb_scene* scenes, int32_t num_scenes, int64_t max_cells,
                          pgb_stream_t stream);
 
-/* One training step over all rays: ray r belongs to scene ray_scene[r] and starts at
+/* No counterpart in the reference (batched form; per ray it is scripts/train.py:130-181).
+ * One training step over all rays: ray r belongs to scene ray_scene[r] and starts at
  * origins[r] along dirs[r]; target[r] is its pixel. scenes is a DEVICE array of
  * num_scenes (<= 256) descriptors. Gradients accumulate into each scene's grad_cells;
  * loss_out[0] = loss_weight * mean over all rays and channels of the squared error.
@@ -241,8 +244,9 @@ int pgb_avg_pool3d_shape(const int32_t dims[3], int32_t window, int32_t stride,
                          int32_t out_dims[3], int64_t* scratch_bytes);
 int pgb_avg_pool3d_fwd(const float* cells, const int32_t dims[3], int32_t window, int32_t stride,
                        void* scratch, float* out, pgb_stream_t stream);
-/* Adjoint: d_cells[X,Y,Z,4] = the pooled gradient spread back over each window (every cell
- * written, so no prior zeroing is needed). */
+/* Adjoint (autograd of F.avg_pool3d at src/grid_functions.py:178): d_cells[X,Y,Z,4] = the
+ * pooled gradient spread back over each window (every cell written, so no prior zeroing
+ * is needed). */
 int pgb_avg_pool3d_bwd(const float* d_out, const int32_t dims[3], int32_t window, int32_t stride,
                        void* scratch, float* d_cells, pgb_stream_t stream);
 
@@ -278,7 +282,9 @@ int pgb_normalize_samples(const float* samples, int64_t count, const float* grid
 int pgb_nearest_gather(const pgb_grid* grid, const void* normalized, int64_t count,
                        void* vals_out, uint8_t* inbounds_out, int64_t* index_out,
                        pgb_stream_t stream);
-/* Backward of pgb_nearest_gather: grad_cells[idx] += d_vals (clip mask applied). */
+/* Backward of pgb_nearest_gather (the index backward that loss.backward() at
+ * scripts/train.py:181 runs through src/grid_functions.py:114): grad_cells[idx] += d_vals
+ * (clip mask applied). */
 int pgb_nearest_scatter(const pgb_grid* grid, const void* normalized, int64_t count,
                         const void* d_vals, void* grad_cells, pgb_stream_t stream);
 
@@ -293,7 +299,8 @@ int pgb_grid_coords(const int32_t dims[3], float points_distance, float* coords_
  * end; an index outside the grid OR-s 1 into status_out and yields zeros. */
 int pgb_gather_cells(const pgb_grid* grid, const int64_t* indices, int64_t count, void* vals_out,
                      int32_t* status_out, pgb_stream_t stream);
-/* Backward of pgb_gather_cells: grad_cells[idx[m]] += d_vals[m] (clip mask applied). */
+/* Backward of pgb_gather_cells (autograd of the gather at src/grid_functions.py:169):
+ * grad_cells[idx[m]] += d_vals[m] (clip mask applied). */
 int pgb_scatter_cells(const pgb_grid* grid, const int64_t* indices, int64_t count,
                       const void* d_vals, void* grad_cells, int32_t* status_out,
                       pgb_stream_t stream);
@@ -317,7 +324,8 @@ int pgb_wrap_indices(int64_t* indices, int64_t count, const int32_t dims[3], pgb
  * reference raises IndexError. */
 int pgb_trilinear_gather(const pgb_grid* grid, const void* normalized, const int64_t* corners,
                          int64_t count, void* out, int32_t* status_out, pgb_stream_t stream);
-/* Backward of pgb_trilinear_gather into grad_cells. */
+/* Backward of pgb_trilinear_gather into grad_cells (autograd of the gathers and blends of
+ * src/grid_functions.py:31-42). */
 int pgb_trilinear_scatter(const pgb_grid* grid, const void* normalized, const int64_t* corners,
                           int64_t count, const void* d_out, void* grad_cells,
                           int32_t* status_out, pgb_stream_t stream);
@@ -326,7 +334,8 @@ int pgb_trilinear_scatter(const pgb_grid* grid, const void* normalized, const in
  * (M = cameras * rays). out[M,4] = (sum w*rgb, sum w), w_k = a_k * prod_{j<k}(1 - a_j). */
 int pgb_composite_fwd(const void* samples, int32_t dtype, int64_t num_rays, int32_t num_samples,
                       void* out, pgb_stream_t stream);
-/* Backward: d_samples[M,S,4] from d_out[M,4] (division-free, exact at alpha == 1). */
+/* Backward (autograd of src/ray_sampling.py:181-188): d_samples[M,S,4] from d_out[M,4]
+ * (division-free, exact at alpha == 1). */
 int pgb_composite_bwd(const void* samples, int32_t dtype, int64_t num_rays, int32_t num_samples,
                       const void* d_out, void* d_samples, pgb_stream_t stream);
 
@@ -367,16 +376,19 @@ int pgb_probe_random_reads(const void* table, int64_t table_bytes, int64_t num_r
 int pgb_probe_random_atomics(void* table, int64_t table_bytes, int64_t num_updates, uint64_t seed,
                              pgb_stream_t stream);
 
-/* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel. */
+/* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel: the
+ * gradient zeroing of optimizer.zero_grad() (scripts/train.py:180) and of a fresh .grad. */
 int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream);
 
 /* The counter-based uniform in [0,1) used for stratification and in-kernel ray
- * generation, evaluated on the host: uniform(seed, a, b). Exact multiples of 2^-24. */
+ * generation, evaluated on the host: uniform(seed, a, b). Exact multiples of 2^-24. No
+ * counterpart in the reference (it draws torch.rand; the drop-in generate_rays_batched
+ * still does). */
 float pgb_hash_uniform(uint64_t seed, uint64_t a, uint32_t b);
 
-/* Number of kernels this library has launched in this process (all entry points). */
+/* Library utilities, no counterpart in the reference: kernels launched in this process
+ * (all entry points), the version string and the text of a status code. */
 int64_t pgb_launch_count(void);
-
 const char* pgb_version(void);
 const char* pgb_status_string(int status);
 
