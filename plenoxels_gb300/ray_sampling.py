@@ -63,14 +63,16 @@ def generate_rays_batched(imgs, number_of_rays, transform_matricies, camera_angl
         uv = _f32(ray_uv, "generate_rays_batched")
     dirs = torch.empty(C * R, 3, dtype=torch.float32, device=T.device)
     pixels = torch.empty(C * R, 4, dtype=torch.float32, device=T.device)
-    status = torch.zeros(1, dtype=torch.int32, device=T.device)
+    # a pixel index can only leave the image for non-square images or caller-given uniforms
+    # (torch.rand draws lie in [0,1)); only then is the status word read back
+    checked = I.shape[1] != I.shape[2] or ray_uv is not None
+    status = torch.zeros(1, dtype=torch.int32, device=T.device) if checked else None
     check(_lib.load().pgb_generate_rays(ptr(T), C, R, float(camera_angle_x), ptr(I), I.shape[1],
                                         I.shape[2], ptr(uv), 1 if even_spread else 0, ptr(dirs),
                                         ptr(pixels), ptr(status), stream_of(T)),
           "generate_rays_batched")
-    if I.shape[1] != I.shape[2] or ray_uv is not None:
-        if int(status.item()) != 0:
-            raise IndexError("generate_rays_batched: pixel index out of range of the images")
+    if checked and int(status.item()) != 0:
+        raise IndexError("generate_rays_batched: pixel index out of range of the images")
     return dirs, pixels
 
 
