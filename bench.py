@@ -42,7 +42,7 @@ WORKLOAD = dict(workload="train step, 256^3 fp32 grid, 100 cams 800x800, 8192 ra
                          "stratified samples, trilinear", grid=256, cameras=100, image=800,
                 rays=8192, samples=256, mode="trilinear", near=2.0, far=6.0, blobs=16,
                 camera_angle_x=0.691)
-NCU_TRAFFIC_BYTES = 446_998_272 + 259_215_872  # DRAM read + write, one launch (rays + next-buffer zeroing)
+NCU_TRAFFIC_BYTES = 446_778_112 + 35_163_904  # DRAM read + write, one launch
 METRIC = "train rays/sec (fwd+bwd)"
 
 
