@@ -619,19 +619,17 @@ def main():
     # traffic: dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on
     # this workload under ncu (profiles/render_train_trilinear_256cube_ncu.md)
     U, inb_frac = unique_cells(pg, grid, T, imgs, W, 1000 * rank + args.warmup, delta, pd)
-    # the launch also zeroes the other 256 MiB gradient buffer for the next step (G * 16 B
-    # written, the dense gradient materialisation the autograd contract requires)
-    alg_bytes = U * 16 + U * 16 + R * 60 + grid.numel() * 4
+    alg_bytes = U * 16 + U * 16 + R * 60
     peak, peak_kind = _peaks()
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
                 "traffic_unit": "bytes per launch (ncu capture of this workload)",
-                "kernel": "render_kernel<trilinear,train> (rays + zeroing of the next gradient buffer)",
+                "kernel": "render_kernel<trilinear,train>",
                 "kernel_ms": kern_ms, "unique_cells": U, "algorithmic_bytes": alg_bytes,
                 "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "issued_gather_bytes": int(R * S * inb_frac * 8 * 16),
-                "step_bytes": alg_bytes}
+                "step_bytes": alg_bytes + grid.numel() * 4}
     line = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",

@@ -138,17 +138,6 @@ int pgb_render_train_terms(const pgb_grid* grid, const pgb_rays* rays, const voi
                            const pgb_loss_terms* terms, void* rgba_out, void* grad_cells,
                            void* losses_out, void* workspace, pgb_stream_t stream);
 
-/* pgb_render_train_terms that also zeroes next_grad_bytes bytes at next_grad (16-byte
- * aligned, a multiple of 16, not overlapping grad_cells) in the same launch: the next
- * step's gradient buffer of a caller that alternates two (the zero_grad of
- * scripts/train.py:180 for the step after this one). The zeroing runs in blocks scheduled
- * after the ray blocks, in the tail the ray blocks leave, instead of a separate fill that
- * competes with the gathers. No counterpart in the reference. */
-int pgb_render_train_zero_next(const pgb_grid* grid, const pgb_rays* rays, const void* target,
-                               const pgb_loss_terms* terms, void* rgba_out, void* grad_cells,
-                               void* losses_out, void* workspace, void* next_grad,
-                               int64_t next_grad_bytes, pgb_stream_t stream);
-
 /* Debug/parity view of the fused kernels' own index math: for every sample of every
  * ray, the wrapped cell indices the lookup reads (nearest: [R,S,3]; trilinear:
  * [R,S,8,3], corner order of src/grid_functions.py:16-24) and the in-bounds flag

@@ -91,8 +91,6 @@ _SIGNATURES = {
     "pgb_render_train": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, c_double, _P, _P, _P, _P, _P]),
     "pgb_train_workspace_bytes": (c_int64, []),
     "pgb_render_train_terms": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, POINTER(PgbLossTerms), _P, _P, _P, _P, _P]),
-    "pgb_render_train_zero_next": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, POINTER(PgbLossTerms), _P, _P,
-                                             _P, _P, _P, c_int64, _P]),
     "pgb_render_train_noalloc": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, c_double, _P, _P, _P, _P]),
     "pgb_render_sample_indices": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P, _P]),
     "pgb_build_bricks": (c_int32, [_P, POINTER(c_int32), c_int32, _P, _P]),

@@ -1,7 +1,6 @@
 // extern "C" entry points of include/plenoxels_gb300.h: argument validation, conversion
 // of the plain-C descriptors into kernel arguments, and dispatch. Nothing here allocates
 // or synchronises.
-#include <algorithm>
 #include <atomic>
 #include <cmath>
 
@@ -145,22 +144,11 @@ int dispatch_render<double>(const pgb_grid* g, const pgb_rays* r, RenderArgs<dou
   return launch_render_f64(a, g->mode, phase, s);
 }
 
-// Blocks that zero the next gradient buffer in a training launch: one per resident block
-// slot of the ray blocks (two per SM), so they fill the tail the ray blocks leave.
-int zero_blocks_for(int64_t n16) {
-  if (n16 <= 0) return 0;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t b = std::min<int64_t>((int64_t)std::max(sms, 1) * 2, kMaxZeroBlocks);
-  return (int)std::max<int64_t>(1, std::min<int64_t>(b, n16));
-}
-
 template <typename Real>
 int render_common(const pgb_grid* g, const pgb_rays* r, int phase, void* rgba_out,
                   const void* d_rgba, const void* target, double loss_w, void* grad,
                   void* loss_out, void* workspace, cudaStream_t s, double beta_w = 0.0,
-                  float beta_eps = 0.f, void* zero_next = nullptr, int64_t zero_bytes = 0) {
+                  float beta_eps = 0.f) {
   RenderArgs<Real> a = render_args<Real>(g, r);
   a.beta_w = beta_w;
   a.beta_eps = beta_eps;
@@ -178,11 +166,6 @@ int render_common(const pgb_grid* g, const pgb_rays* r, int phase, void* rgba_ou
   }
   a.loss_w = loss_w;
   a.inv_count = r->num_rays > 0 ? 1.0 / (4.0 * (double)r->num_rays) : std::nan("");
-  if (phase == kTrain && zero_next != nullptr && zero_bytes > 0) {
-    a.zero_ptr = reinterpret_cast<float4*>(zero_next);
-    a.zero_n16 = zero_bytes / 16;
-    a.zero_blocks = zero_blocks_for(a.zero_n16);
-  }
   return dispatch_render<Real>(g, r, a, phase, s);
 }
 
@@ -258,35 +241,6 @@ int pgb_render_train_terms(const pgb_grid* grid, const pgb_rays* rays, const voi
   return render_common<float>(grid, rays, kTrain, rgba_out, nullptr, target, terms->mse_weight,
                               grad_cells, losses_out, workspace, stream, terms->beta_weight,
                               terms->beta_eps);
-}
-
-int pgb_render_train_zero_next(const pgb_grid* grid, const pgb_rays* rays, const void* target,
-                               const pgb_loss_terms* terms, void* rgba_out, void* grad_cells,
-                               void* losses_out, void* workspace, void* next_grad,
-                               int64_t next_grad_bytes, pgb_stream_t stream) {
-  if (!terms || next_grad_bytes < 0) return PGB_ERR_ARG;
-  int st = check_grid(grid);
-  if (st) return st;
-  if ((st = check_rays(grid, rays, true))) return st;
-  if (!grad_cells || !losses_out || !workspace) return PGB_ERR_ARG;
-  if (!rays->cameras && rays->num_rays > 0 && !target) return PGB_ERR_ARG;
-  if (!aligned(grad_cells, 16) || !aligned(workspace, 16)) return PGB_ERR_ALIGN;
-  if (next_grad_bytes > 0) {
-    if (!next_grad) return PGB_ERR_ARG;
-    if (!aligned(next_grad, 16) || next_grad_bytes % 16 != 0) return PGB_ERR_ALIGN;
-    const char* n0 = static_cast<const char*>(next_grad);
-    const char* g0 = static_cast<const char*>(grad_cells);
-    const int64_t gbytes = (int64_t)grid->dims[0] * grid->dims[1] * grid->dims[2] * 4 *
-                           (grid->dtype == PGB_F64 ? 8 : 4);
-    if (n0 < g0 + gbytes && g0 < n0 + next_grad_bytes) return PGB_ERR_ARG;  // overlap
-  }
-  if (grid->dtype == PGB_F64)
-    return render_common<double>(grid, rays, kTrain, rgba_out, nullptr, target, terms->mse_weight,
-                                 grad_cells, losses_out, workspace, stream, terms->beta_weight,
-                                 terms->beta_eps, next_grad, next_grad_bytes);
-  return render_common<float>(grid, rays, kTrain, rgba_out, nullptr, target, terms->mse_weight,
-                              grad_cells, losses_out, workspace, stream, terms->beta_weight,
-                              terms->beta_eps, next_grad, next_grad_bytes);
 }
 
 int pgb_render_sample_indices(const pgb_grid* grid, const pgb_rays* rays, int64_t* index_out,

@@ -16,8 +16,6 @@ int after_launch();
 
 // Most warps the fused training kernel may use (size of its per-warp loss table).
 constexpr int kMaxTrainWarps = 32768;
-// Most blocks a training launch may add to zero the next gradient buffer.
-constexpr int kMaxZeroBlocks = 1024;
 // Samples per chunk are 32 * K; a ray may span at most this many chunks.
 constexpr int kMaxChunks = 32;
 // Largest samples-per-ray the fused kernels accept.

@@ -78,12 +78,6 @@ struct RenderArgs {
   float beta_eps;
   double inv_samples;
   double* partials_beta;
-  // training phase: the last zero_blocks blocks of the grid zero zero_n16 16-byte words
-  // at zero_ptr (the next step's gradient buffer) instead of rendering rays; they are
-  // scheduled after the ray blocks, into the tail where ray blocks leave SMs idle
-  float4* zero_ptr;
-  int64_t zero_n16;
-  int zero_blocks;
 };
 
 template <typename Real>
@@ -507,10 +501,8 @@ render_kernel(const RenderArgs<Real> a) {
   constexpr bool ADJ = PHASE != kForward;
   const int lane = threadIdx.x & (kWarp - 1);
   const int warps_per_block = blockDim.x >> 5;
-  const int ray_blocks = (int)gridDim.x - (PHASE == kTrain ? a.zero_blocks : 0);
-  const bool zero_block = (int)blockIdx.x >= ray_blocks;
-  const int64_t gw = zero_block ? a.R : (int64_t)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
-  const int64_t nw = (int64_t)ray_blocks * warps_per_block;
+  const int64_t gw = (int64_t)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const int64_t nw = (int64_t)gridDim.x * warps_per_block;
   const int nchunks = (a.S + kWarp * K - 1) / (kWarp * K);
   CoordStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
   double loss_lane = 0.0;
@@ -669,14 +661,6 @@ render_kernel(const RenderArgs<Real> a) {
         }
       }
     }
-  }
-
-  if (PHASE == kTrain && zero_block) {  // this block's slice of the next gradient buffer
-    const int64_t per = (a.zero_n16 + a.zero_blocks - 1) / a.zero_blocks;
-    const int64_t lo = (int64_t)(blockIdx.x - ray_blocks) * per;
-    const int64_t hi = lo + per < a.zero_n16 ? lo + per : a.zero_n16;
-    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-      a.zero_ptr[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 
   if (PHASE == kTrain) {

@@ -28,10 +28,9 @@ int launch_render_k(const RenderArgs<Real>& a, cudaStream_t s) {
     configured[dev] = 1;
   }
   int64_t blocks = (a.R + kWarpsPerBlock - 1) / kWarpsPerBlock;
-  blocks = std::min<int64_t>(blocks, PHASE == kTrain ? kMaxTrainWarps / kWarpsPerBlock - kMaxZeroBlocks
+  blocks = std::min<int64_t>(blocks, PHASE == kTrain ? kMaxTrainWarps / kWarpsPerBlock
                                                      : (int64_t)1 << 20);
   if (blocks < 1) blocks = 1;
-  if (PHASE == kTrain) blocks += a.zero_blocks;  // zeroing blocks after the ray blocks
   render_kernel<Real, Store, MODE, K, PHASE, LOGT><<<(unsigned)blocks, kThreads, kSmem, s>>>(a);
   return after_launch();
 }

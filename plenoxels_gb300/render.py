@@ -194,11 +194,10 @@ class FusedTrainStep:
     unless zero_grad=False, in which case it accumulates like autograd does. Every call
     is asynchronous; the returned loss is a device scalar.
 
-    overlap_zero=True keeps two gradient buffers: each launch accumulates into the buffer
-    the previous launch zeroed and zeroes the other one in blocks that run in its own tail
-    (pgb_render_train_zero_next), so the 256 MiB fill of a 256^3 grid is neither a
-    separate pass nor a competitor of the gathers. A step's gradient then stays valid until
-    the next step is launched; the buffer alternates, and ``grid.grad``/``self.grad`` follow.
+    overlap_zero=True keeps two gradient buffers and zeroes the next step's buffer on a
+    side stream while the current step's kernel runs (the 256 MiB fill of a 256^3 grid
+    no longer sits on the critical path). A step's gradient then stays valid until the
+    next step is launched; the buffer alternates, and ``grid.grad``/``self.grad`` follow.
     """
 
     def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
@@ -229,9 +228,11 @@ class FusedTrainStep:
         dev = grid.device
         self.workspace = torch.zeros(lib.pgb_train_workspace_bytes(), dtype=torch.uint8, device=dev)
         self._grads = [torch.zeros(grid.shape, dtype=self.real, device=dev)]
-        self._double = bool(overlap_zero)
-        if self._double:
+        self._side = None
+        if overlap_zero:
             self._grads.append(torch.zeros(grid.shape, dtype=self.real, device=dev))
+            self._side = torch.cuda.Stream(device=dev)
+            self._zeroed = [None, None]  # event: buffer b is zero and free
         self._cur = 0
         self.grad = self._grads[0]
         # losses[0]: loss_weight * MSE; losses[1]: the beta term (scripts/train.py:170-177)
@@ -250,38 +251,43 @@ class FusedTrainStep:
                                         stream.cuda_stream), "train step")
 
     def _gradient_for_step(self, zero_grad):
-        """(buffer this step accumulates into, buffer to zero in the same launch or None)."""
         main = torch.cuda.current_stream(self.grid.device)
         if not zero_grad:
-            return self.grad, None
-        if not self._double:
+            return self.grad
+        if self._side is None:
             self._fill(self.grad, main)
-            return self.grad, None
-        # two buffers: this step accumulates into the one the previous launch zeroed and
-        # zeroes the other (the previous step's gradient, consumed by then in stream order)
+            return self.grad
         b = self._cur
-        buf, other = self._grads[b], self._grads[1 - b]
-        self._cur = 1 - b
+        buf = self._grads[b]
+        if self._zeroed[b] is None:
+            self._fill(buf, main)
+        else:
+            main.wait_event(self._zeroed[b])
+        # zero the other buffer for the next step, after everything already queued on the
+        # main stream (its last reader, e.g. the optimizer step of the previous step)
+        o = 1 - b
+        ready = torch.cuda.Event()
+        ready.record(main)
+        self._side.wait_event(ready)
+        self._fill(self._grads[o], self._side)
+        done = torch.cuda.Event()
+        done.record(self._side)
+        self._zeroed[o] = done
+        self._cur = o
         self.grad = buf
         self._attach()
-        return buf, other
+        return buf
 
     def _launch(self, rdesc, target, rgba_out, zero_grad):
         lib = _lib.load()
-        grad, zero_next = self._gradient_for_step(zero_grad)
+        grad = self._gradient_for_step(zero_grad)
         stream = torch.cuda.current_stream(self.grid.device)
         gdesc = _lib.make_grid(self.grid, self.grid_min, self.points_distance, self.mode, self.clip)
         ev = None
         if self.kernel_events is not None:
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record(stream)
-        if zero_next is not None:
-            terms = _lib.PgbLossTerms(self.loss_weight, self.beta, self.beta_eps)
-            check(lib.pgb_render_train_zero_next(gdesc, rdesc, ptr(target), terms, ptr(rgba_out),
-                                                 ptr(grad), ptr(self.losses), ptr(self.workspace),
-                                                 ptr(zero_next), zero_next.numel() * zero_next.element_size(),
-                                                 stream.cuda_stream), "train step")
-        elif self.beta == 0.0:
+        if self.beta == 0.0:
             check(lib.pgb_render_train(gdesc, rdesc, ptr(target), self.loss_weight, ptr(rgba_out),
                                        ptr(grad), ptr(self.losses), ptr(self.workspace),
                                        stream.cuda_stream), "train step")

@@ -120,15 +120,6 @@ def test_argument_validation_without_launch(lib):
     assert lib.pgb_render_fwd(ctypes.byref(g), ctypes.byref(r), 16, None) == _lib.PGB_ERR_ARG  # no rays
     assert lib.pgb_render_train(ctypes.byref(g), ctypes.byref(r), None, 1.0, None, None, None, None,
                                 None) == _lib.PGB_ERR_ARG
-    # the next-gradient buffer of pgb_render_train_zero_next: aligned, whole words, apart
-    r.num_rays = 4
-    r.origins, r.dirs = 256, 256
-    terms = _lib.PgbLossTerms(1.0, 0.0, 1e-4)
-    gbytes = 4 * 4 * 4 * 4 * 4
-    assert lib.pgb_render_train_zero_next(ctypes.byref(g), ctypes.byref(r), 256, ctypes.byref(terms), None,
-                                          4096, 512, 8192, 4096 + 16, gbytes, None) == _lib.PGB_ERR_ARG
-    assert lib.pgb_render_train_zero_next(ctypes.byref(g), ctypes.byref(r), 256, ctypes.byref(terms), None,
-                                          4096, 512, 8192, 1 << 20, 40, None) == _lib.PGB_ERR_ALIGN
     assert lib.pgb_wrap_indices(None, 3, None, None) == _lib.PGB_ERR_ARG
     assert lib.pgb_fill_zero(24, 16, None) == _lib.PGB_ERR_ALIGN
     assert lib.pgb_probe_random_reads(None, 256, 8, 1, 16, None) == _lib.PGB_ERR_ARG
