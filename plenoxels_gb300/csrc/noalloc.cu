@@ -9,10 +9,9 @@
 // library, so the call needs only the inputs and outputs.
 #include <cmath>
 #include <mutex>
-#include <type_traits>
 
 #include "pgb_host.h"
-#include "render.cuh"
+#include "render_args.cuh"
 
 namespace pgb {
 namespace {
@@ -51,41 +50,15 @@ int scratch_address(void** out) {
   return PGB_OK;
 }
 
-inline bool aligned_to(const void* p, uintptr_t a) { return ((uintptr_t)p % a) == 0; }
-
 template <typename Real>
 int launch_noalloc(const pgb_grid* g, const pgb_rays* r, const void* target, double loss_weight,
                    void* rgba_out, void* grad_cells, void* loss_out, unsigned char* scratch,
                    cudaStream_t stream) {
-  RenderArgs<Real> a = {};
-  a.g.cells = g->cells;
-  a.g.X = g->dims[0]; a.g.Y = g->dims[1]; a.g.Z = g->dims[2];
-  a.g.fX = (Real)a.g.X; a.g.fY = (Real)a.g.Y; a.g.fZ = (Real)a.g.Z;
-  a.g.ox = (Real)g->origin[0]; a.g.oy = (Real)g->origin[1]; a.g.oz = (Real)g->origin[2];
-  a.g.pd = (Real)g->points_distance;
-  a.g.clip = g->clip ? 1 : 0;
-  a.origins = (const Real*)r->origins;
-  a.dirs = (const Real*)r->dirs;
-  if (r->cameras) {
-    const pgb_cameras* c = r->cameras;
-    a.use_cameras = 1;
-    a.transforms = c->transforms;
-    a.images = c->images;
-    a.C = c->num_cameras;
-    a.H = c->height;
-    a.W = c->width;
-    a.fov = c->camera_angle_x;
-    a.near_dist = c->near;
-    a.cam_seed = c->seed;
-  }
-  a.R = r->num_rays;
-  a.S = r->num_samples;
-  a.delta = (Real)r->delta_step;
-  a.stratified = r->stratified ? 1 : 0;
-  a.strat_seed = r->seed;
-  a.term_thr = r->term_threshold;
-  a.use_bg = r->use_background ? 1 : 0;
-  for (int c = 0; c < 3; ++c) a.bg[c] = r->background[c];
+  // the same kernel arguments as pgb_render_train (render_args.cuh), with the loss
+  // partials and the block counter in the library's scratch instead of a workspace
+  RenderArgs<Real> a = render_args<Real>(g, r);
+  const double samples = (double)r->num_rays * (double)r->num_samples;
+  a.inv_samples = samples > 0 ? 1.0 / samples : std::nan("");
   a.rgba_out = (Real*)rgba_out;
   a.target = (const Real*)target;
   a.grad = (Real*)grad_cells;
@@ -94,12 +67,7 @@ int launch_noalloc(const pgb_grid* g, const pgb_rays* r, const void* target, dou
   a.counter = (unsigned*)(scratch + kCounterOffset);
   a.loss_w = loss_weight;
   a.inv_count = r->num_rays > 0 ? 1.0 / (4.0 * (double)r->num_rays) : std::nan("");
-  if constexpr (std::is_same<Real, double>::value) {
-    return launch_render_f64(a, g->mode, kTrain, stream);
-  } else {
-    if (g->dtype == PGB_BF16) return launch_render_bf16(a, g->mode, kTrain, stream);
-    return launch_render_f32(a, g->mode, kTrain, stream);
-  }
+  return dispatch_render<Real>(g, r, a, kTrain, stream);
 }
 
 }  // namespace
@@ -111,33 +79,17 @@ extern "C" int pgb_render_train_noalloc(const pgb_grid* grid, const pgb_rays* ra
                                         const void* target, double loss_weight, void* rgba_out,
                                         void* grad_cells, void* loss_out, pgb_stream_t stream) {
   // the same argument rules as pgb_render_train
-  if (!grid || !grid->cells || !rays) return PGB_ERR_ARG;
-  if (grid->dtype != PGB_F32 && grid->dtype != PGB_BF16 && grid->dtype != PGB_F64) return PGB_ERR_ARG;
-  if (grid->mode != PGB_NEAREST && grid->mode != PGB_TRILINEAR) return PGB_ERR_ARG;
-  if (grid->dims[0] <= 0 || grid->dims[1] <= 0 || grid->dims[2] <= 0) return PGB_ERR_ARG;
-  if ((uint64_t)grid->dims[0] * grid->dims[1] * grid->dims[2] >= (1ull << 40)) return PGB_ERR_UNSUPPORTED;
-  if (!aligned_to(grid->cells, grid->dtype == PGB_BF16 ? 8 : 16)) return PGB_ERR_ALIGN;
-  if (rays->num_rays < 0 || rays->num_samples < 0) return PGB_ERR_ARG;
-  if (rays->num_samples > kMaxSamples) return PGB_ERR_UNSUPPORTED;
-  if (rays->log_transmittance) return PGB_ERR_UNSUPPORTED;  // product-scan form only
+  int st = check_grid(grid);
+  if (st) return st;
+  if ((st = check_rays(grid, rays, true))) return st;
   // the scratch holds the loss partials of at most PGB_NOALLOC_MAX_RAYS rays per call
   if (rays->num_rays > PGB_NOALLOC_MAX_RAYS) return PGB_ERR_UNSUPPORTED;
-  if (rays->cameras) {
-    const pgb_cameras* c = rays->cameras;
-    if (grid->dtype == PGB_F64) return PGB_ERR_UNSUPPORTED;
-    if (!c->transforms || !c->images || c->num_cameras <= 0 || c->height <= 0 || c->width <= 0)
-      return PGB_ERR_ARG;
-    if (c->height != c->width) return PGB_ERR_UNSUPPORTED;
-    if (!aligned_to(c->images, 16)) return PGB_ERR_ALIGN;
-  } else if (rays->num_rays > 0 && (!rays->origins || !rays->dirs || !target)) {
-    return PGB_ERR_ARG;
-  }
   if (!grad_cells || !loss_out) return PGB_ERR_ARG;
-  if (!aligned_to(grad_cells, 16)) return PGB_ERR_ALIGN;
+  if (!rays->cameras && rays->num_rays > 0 && !target) return PGB_ERR_ARG;
+  if (!aligned(grad_cells, 16)) return PGB_ERR_ALIGN;
 
   void* scratch = nullptr;
-  int st = scratch_address(&scratch);
-  if (st) return st;
+  if ((st = scratch_address(&scratch))) return st;
   // the block counter must start at zero; every partial is written before it is read
   if (cudaMemsetAsync((unsigned char*)scratch + kCounterOffset, 0, sizeof(unsigned), stream) !=
       cudaSuccess)
