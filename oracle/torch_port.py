@@ -159,6 +159,16 @@ def corner_indices(n):
     return torch.cat(pts, 1).type(torch.long)
 
 
+def collect_cells(n, grid):
+    """src/grid_functions.py:154-170 collect_cell_information_via_indices: the in-bounds
+    mask of the float coordinates, then the 8 corners flattened to [N*8,3], wrapped in
+    place and gathered. Returns (values [N*8,4], mask [N])."""
+    mask = in_bounds(n, grid.shape)
+    corners = corner_indices(n).reshape(-1, 3)
+    wrap_(corners, grid.shape)
+    return grid[corners[:, 0], corners[:, 1], corners[:, 2]], mask
+
+
 def trilinear_blend(n, corners, grid):
     """src/grid_functions.py:7-44 trilinear_interpolation, same op order."""
     fr = torch.frac(n)
@@ -299,8 +309,10 @@ def remove_noise(grid_cells, kernel_size=3, radius=1.0, threshold=2, repeats=20)
 
 
 def splat_preview(grid, points_distance, transform_matrix, camera_angle_x, size_y):
-    """src/visualization.py:157-232 (visulize_3d_in_2d_fast), same ops; returns the image,
-    the pixel of every drawn point and its distance."""
+    """src/visualization.py:157-232 (visulize_3d_in_2d_fast), same ops. Returns the image
+    and, per drawn point (points inside the field of view), a dict of its pixel (xx, yy),
+    its unrounded pixel coordinates (fx = xs * x_norm, fy = size_y * y_norm), its
+    normalised coordinates (xn, yn) and its distance from the camera."""
     rot = transform_matrix[:3, :3]
     pos = transform_matrix[:3, 3]
     yz = transform_matrix[:3, 0]
@@ -323,10 +335,11 @@ def splat_preview(grid, points_distance, transform_matrix, camera_angle_x, size_
     xn, yn, colors, ctp = xn[ok], yn[ok], colors[ok], ctp[ok]
     ys = size_y
     xs = int(ys * aspect)
-    xx = (xs * xn).round().clamp(min=0, max=xs - 1).type(torch.long)
-    yy = (ys * yn).round().clamp(min=0, max=ys - 1).type(torch.long)
+    fx, fy = xs * xn, ys * yn
+    xx = fx.round().clamp(min=0, max=xs - 1).type(torch.long)
+    yy = fy.round().clamp(min=0, max=ys - 1).type(torch.long)
     dist = ctp.norm(dim=1)
     order = torch.argsort(-dist)
     img = np.ones([xs, ys, 3])
     img[xx[order], yy[order]] = colors[order][:, :3]
-    return img, xx, yy, dist
+    return img, dict(xx=xx, yy=yy, fx=fx, fy=fy, xn=xn, yn=yn, dist=dist)

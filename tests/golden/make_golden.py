@@ -1,12 +1,13 @@
 """Generates the golden fixtures in this folder by running the REFERENCE's own functions
-(DanJbk/Plenoxels, read from /root/reference) on seeded synthetic inputs, on CPU.
+(DanJbk/Plenoxels) on seeded synthetic inputs, on CPU.
 
-Run in the build container (the GPU machine has no copy of the reference):
-    python tests/golden/make_golden.py
+Run where a checkout of the reference exists, naming its root directory:
+    PLENOXELS_REFERENCE=<path to the reference checkout> python tests/golden/make_golden.py
 
-The reference imports PIL through src/data_processing.py:3 only to read PNG files; a
-stub module stands in for it (no reference file is modified). Each fixture stores the
-inputs, the reference's outputs and the reference autograd gradient.
+The reference imports PIL through src/data_processing.py:3 only to read PNG files, and
+src/visualization.py imports matplotlib and plotly only for its plots; stub modules stand
+in for them (no reference file is modified, and no stubbed function is called). Each
+fixture stores the inputs, the reference's outputs and the reference autograd gradient.
 """
 from __future__ import annotations
 
@@ -18,18 +19,30 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("PLENOXELS_REFERENCE", "/root/reference")
+REF = os.environ.get("PLENOXELS_REFERENCE")
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    sys.exit("set PLENOXELS_REFERENCE to the root of a DanJbk/Plenoxels checkout")
 sys.path.insert(0, os.path.dirname(HERE))  # tests/
 sys.modules.setdefault("PIL", types.ModuleType("PIL"))
 sys.modules["PIL"].Image = None
+# plotting modules of src/visualization.py:1-6 (only its plot functions use them)
+for _name in ("matplotlib", "matplotlib.pyplot", "matplotlib.colors", "plotly",
+              "plotly.graph_objs", "plotly.io"):
+    sys.modules.setdefault(_name, types.ModuleType(_name))
+sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+sys.modules["matplotlib"].colors = sys.modules["matplotlib.colors"]
+sys.modules["plotly"].graph_objs = sys.modules["plotly.graph_objs"]
+sys.modules["plotly"].io = sys.modules["plotly.io"]
 sys.path.insert(0, REF)
 
 import scenes  # noqa: E402
-from src.grid_functions import (fix_out_of_bounds, find_out_of_bound, generate_grid,  # noqa: E402
-                                get_grid_points_indices, get_nearest_voxels,
-                                trilinear_interpolation)
+from src.grid_functions import (collect_cell_information_via_indices,  # noqa: E402
+                                convolve_grid_to_remove_noise, fix_out_of_bounds,
+                                find_out_of_bound, generate_grid, get_grid_points_indices,
+                                get_nearest_voxels, trilinear_interpolation)
 from src.ray_sampling import (compute_alpha_weighted_pixels, normalize_samples_for_indecies,  # noqa: E402
                               sample_camera_rays_batched)
+from src.visualization import visulize_3d_in_2d_fast  # noqa: E402
 
 
 def _np(t):
@@ -134,6 +147,56 @@ def edge_case(mode):
                 vals=_np(vals), rgba=_np(px), loss=_np(loss), grad=_np(cells.grad))
 
 
+def collect_cells_case(seed):
+    """collect_cell_information_via_indices (src/grid_functions.py:154-170) on a non-cubic
+    grid: coordinates inside, on integer values, in (dim-1, dim) (upper-face wrap),
+    negative and beyond the grid, and the autograd gradient of its gathered values."""
+    rng = np.random.default_rng(seed)
+    dims = (7, 5, 6)
+    grid = rng.uniform(-0.2, 1.2, dims + (4,)).astype(np.float32)
+    n = rng.uniform(-1.5, 1.0, (160, 3)) * np.array(dims) + np.array(dims) * 0.25
+    n[:20] = np.round(n[:20])                                 # integer coordinates
+    n[20:40] = np.array(dims) - rng.uniform(0.0, 1.0, (20, 3))  # upper faces
+    n[40] = [-0.5, 2.5, 3.0]                                  # negative fraction
+    n = n.astype(np.float32)
+    B = torch.from_numpy(grid.copy()).requires_grad_(True)
+    vals, mask = collect_cell_information_via_indices(torch.from_numpy(n.copy()), B)
+    dout = rng.standard_normal(vals.shape).astype(np.float32)
+    vals.backward(torch.from_numpy(dout))
+    return dict(grid=grid, normalized=n, vals=_np(vals), mask=_np(mask), dvals=dout,
+                grad=_np(B.grad))
+
+
+def remove_noise_case(seed):
+    """convolve_grid_to_remove_noise (src/grid_functions.py:270-280) for three kernels."""
+    rng = np.random.default_rng(seed)
+    grid = rng.random((20, 18, 22, 4)).astype(np.float32)
+    keep = rng.random((20, 18, 22)) < 0.4
+    grid[..., 3] = np.where(keep, rng.random((20, 18, 22)), 0.0).astype(np.float32)
+    out = dict(grid=grid)
+    for i, (k, r, t) in enumerate([(3, 1.0, 2.0), (5, 1.5, 3.0), (3, 2.0, 4.5)]):
+        g = torch.from_numpy(grid.copy())
+        res = convolve_grid_to_remove_noise(g, kernel_size=k, radius=r, threshold=t, repeats=6)
+        out[f"params_{i}"] = np.array([k, r, t])
+        out[f"out_{i}"] = _np(res)
+    return out
+
+
+def splat_case(seed):
+    """visulize_3d_in_2d_fast (src/visualization.py:157-232) of a 48^3 blob grid."""
+    side = 48
+    grid = scenes.make_grid(side, 4, seed, amp=(0.05, 0.6))
+    grid[grid[..., 3] <= 0.1] = 0.0  # cells the preview never draws: zeros compress
+    T = scenes.make_cameras(2, seed + 1)
+    out = dict(grid=grid, transforms=T, points_distance=scenes.points_distance(side),
+               camera_angle_x=0.691, size_y=64)
+    for c in range(T.shape[0]):
+        img = visulize_3d_in_2d_fast(torch.from_numpy(grid), scenes.points_distance(side),
+                                     torch.from_numpy(T[c]), 0.691, 64)
+        out[f"img_{c}"] = np.asarray(img)
+    return out
+
+
 def main():
     torch.set_num_threads(1)
     cases = {}
@@ -152,6 +215,9 @@ def main():
     cases["ref_edge_nearest"] = edge_case("nearest")
     cases["ref_edge_trilinear"] = edge_case("trilinear")
     cases["ref_composite"] = composite_case(21)
+    cases["ref_collect_cells"] = collect_cells_case(31)
+    cases["ref_remove_noise"] = remove_noise_case(32)
+    cases["ref_splat"] = splat_case(33)
     for name, d in cases.items():
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})

@@ -130,3 +130,16 @@ def test_generate_grid_matches_reference_layout():
     np.testing.assert_array_equal(coords.min(0)[0].cpu().numpy(), d["grid_min"])
     assert mesh.dtype == torch.int64 and tuple(mesh[1, 2, 3].tolist()) == (1, 2, 3)
     assert coords.data_ptr() == gg.data_ptr()
+
+
+def test_collect_cells_matches_reference():
+    """collect_cell_information_via_indices (src/grid_functions.py:154-170) against the
+    reference's own output: gathered corner values and the float-coordinate mask bit for
+    bit, and the autograd gradient of the gathered values."""
+    d = load_golden("ref_collect_cells")
+    grid = _t(d["grid"]).requires_grad_(True)
+    vals, mask = pg.collect_cell_information_via_indices(_t(d["normalized"]), grid)
+    vals.backward(_t(d["dvals"]))
+    np.testing.assert_array_equal(vals.detach().cpu().numpy(), d["vals"])
+    np.testing.assert_array_equal(mask.cpu().numpy(), d["mask"])
+    _grad_close(grid.grad.cpu().numpy(), d["grad"])

@@ -77,3 +77,98 @@ def test_fixtures_cover_edge_cases():
     s = load_golden("ref_trilinear_saturated")
     assert (s["grid"][..., 3] > 1).sum() > 0, "alpha saturation after the clip"
     assert ((s["grid"] < 0) | (s["grid"] > 1)).sum() > 0
+
+
+def test_oracle_collect_cells_matches_reference():
+    """src/grid_functions.py:154-170: the wrapped 8-corner gather, its mask on the float
+    coordinates and the autograd scatter of its values."""
+    d = load_golden("ref_collect_cells")
+    grid = torch.from_numpy(d["grid"]).requires_grad_(True)
+    vals, mask = tp.collect_cells(torch.from_numpy(d["normalized"]), grid)
+    vals.backward(torch.from_numpy(d["dvals"]))
+    np.testing.assert_array_equal(vals.detach().numpy(), d["vals"])
+    np.testing.assert_array_equal(mask.numpy(), d["mask"])
+    np.testing.assert_allclose(grid.grad.numpy(), d["grad"], rtol=1e-6, atol=1e-6)
+    n = d["normalized"]
+    dims = np.array(d["grid"].shape[:3])
+    assert (~d["mask"]).sum() > 0 and d["mask"].sum() > 0
+    assert ((n > dims - 1) & (n < dims)).any(), "upper-face wrap"
+    assert (n == np.floor(n)).all(axis=1).any(), "integer coordinates"
+
+
+def test_oracle_remove_noise_matches_reference():
+    d = load_golden("ref_remove_noise")
+    for i in range(3):
+        k, r, t = d[f"params_{i}"]
+        got = tp.remove_noise(torch.from_numpy(d["grid"].copy()), int(k), float(r), float(t),
+                              repeats=6)
+        np.testing.assert_array_equal(got.numpy(), d[f"out_{i}"])
+    assert not np.array_equal(d["out_0"], d["grid"]), "the clean-up must clear something"
+
+
+def _splat_ref(d, c):
+    T = torch.from_numpy(d["transforms"][c])
+    return tp.splat_preview(torch.from_numpy(d["grid"]), float(d["points_distance"]), T,
+                            float(d["camera_angle_x"]), int(d["size_y"]))
+
+
+def nearest_wins_image(info, colors_of, shape):
+    """The preview painted by the rule the GPU kernel implements: at each pixel the point
+    nearest to the camera; also returns the pixels where the two nearest points' distances
+    tie (where the reference's unstable far-to-near sort may let either win)."""
+    img = np.ones(shape)
+    best = {}
+    ties = set()
+    xx, yy, dist = info["xx"].numpy(), info["yy"].numpy(), info["dist"].numpy()
+    for i in range(len(xx)):
+        p = (int(xx[i]), int(yy[i]))
+        if p not in best or dist[i] < dist[best[p]]:
+            if p in best and dist[i] == dist[best[p]]:
+                ties.add(p)
+            best[p] = i
+        elif dist[i] == dist[best[p]]:
+            ties.add(p)
+    for p, i in best.items():
+        img[p] = colors_of(i)
+    return img, ties
+
+
+def test_oracle_splat_matches_reference_and_the_nearest_wins_rule():
+    """The oracle's preview equals the reference's image bit for bit, and so do the
+    per-point projections it returns; painting each pixel with its nearest point (the rule
+    the GPU kernel follows) reproduces the reference's far-to-near painter everywhere but at
+    exact distance ties."""
+    d = load_golden("ref_splat")
+    for c in range(d["transforms"].shape[0]):
+        img, info = _splat_ref(d, c)
+        np.testing.assert_array_equal(img, d[f"img_{c}"])
+        grid = torch.from_numpy(d["grid"])
+        cells = grid[grid[..., 3] > 0.1]
+        ok = ((info["xn"] < 1) & (info["xn"] >= 0) & (info["yn"] < 1) & (info["yn"] >= 0))
+        assert bool(ok.all())
+        drawn = cells[:, :3].double().numpy()
+        # points inside the view, in the order splat_preview keeps them
+        inside = np.nonzero(_fov_mask(d, c))[0]
+        painted, ties = nearest_wins_image(info, lambda i: drawn[inside[i]], img.shape)
+        differ = np.argwhere(np.any(painted != img, axis=-1))
+        assert all(tuple(p) in ties for p in differ), "a pixel differs without a distance tie"
+        assert (~np.all(img == 1.0, axis=-1)).sum() > 100
+
+
+def _fov_mask(d, c):
+    """Which of the drawn cells (alpha > 0.1, row-major) project inside the view (the
+    reference's unfitxy filter, src/visualization.py:198-208), from the oracle's ops."""
+    grid = torch.from_numpy(d["grid"])
+    T = torch.from_numpy(d["transforms"][c])
+    pts = np.argwhere(grid[..., 3] > 0.1)
+    half = (torch.tensor(grid.shape[:3]) / 2).unsqueeze(1).ceil()
+    pts = ((pts - half) + 1) * float(d["points_distance"])
+    ctp = pts.T - T[:3, 3]
+    yz, xz = T[:3, 0], T[:3, 1]
+    aspect = yz.norm(dim=0) / xz.norm(dim=0)
+    nm = ctp.norm(dim=1) * yz.norm()
+    ax, ay = torch.matmul(ctp, yz) / nm, torch.matmul(ctp, xz) / nm
+    fov = float(d["camera_angle_x"])
+    xn = 0.5 + ay / -fov
+    yn = 0.5 + ax / (fov / aspect)
+    return ((xn < 1.0) & (xn >= 0.0) & (yn < 1.0) & (yn >= 0.0)).numpy()
