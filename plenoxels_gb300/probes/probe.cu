@@ -1,13 +1,14 @@
-// Device-memory probes behind the render kernels' roofline: the rate at which this GPU
-// serves independent random 32 B sectors (reads, and float4 atomic adds) out of a buffer
-// larger than L2. The fused kernels read one grid cell per trilinear corner and add one
-// gradient cell per corner at positions with no reuse across rays, so this rate, not the
-// streaming copy bandwidth, is the ceiling they run against. No counterpart in the
-// reference; bench.py reports it next to the copy-bandwidth roofline.
+// Device-memory probes, a measurement helper built as its own library (libpgb_probes.so)
+// beside the renderer: the rate at which this GPU serves independent random 32 B sectors
+// (reads, and float4 atomic adds) out of a buffer larger than L2. The fused kernels read
+// one grid cell per trilinear corner and add one gradient cell per corner at positions
+// with little reuse across rays, so this rate, not the streaming copy bandwidth, is what
+// random cell traffic runs against. The benchmark reports it next to the copy-bandwidth
+// roofline. No counterpart in the reference.
 #include <algorithm>
 
-#include "pgb_host.h"
 #include "pgb_device.cuh"
+#include "pgb_probes.h"
 
 namespace pgb {
 namespace {
@@ -43,6 +44,8 @@ __global__ void probe_atomics_kernel(float4* table, uint64_t slots, int64_t n, u
   }
 }
 
+int launch_status() { return cudaGetLastError() == cudaSuccess ? PGB_OK : PGB_ERR_LAUNCH; }
+
 unsigned probe_blocks() {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -65,7 +68,7 @@ int pgb_probe_random_reads(const void* table, int64_t table_bytes, int64_t num_r
   if (((uintptr_t)table % 16) != 0) return PGB_ERR_ALIGN;
   probe_reads_kernel<<<probe_blocks(), 256, 0, stream>>>(
       static_cast<const float4*>(table), (uint64_t)(table_bytes / 16), num_reads, seed, sink);
-  return after_launch();
+  return launch_status();
 }
 
 int pgb_probe_random_atomics(void* table, int64_t table_bytes, int64_t num_updates, uint64_t seed,
@@ -76,7 +79,7 @@ int pgb_probe_random_atomics(void* table, int64_t table_bytes, int64_t num_updat
   if (((uintptr_t)table % 16) != 0) return PGB_ERR_ALIGN;
   probe_atomics_kernel<<<probe_blocks(), 256, 0, stream>>>(
       static_cast<float4*>(table), (uint64_t)(table_bytes / 16), num_updates, seed);
-  return after_launch();
+  return launch_status();
 }
 
 }  // extern "C"

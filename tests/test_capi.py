@@ -40,9 +40,10 @@ def test_struct_layout_matches_header(tmp_path):
         " offsetof(pgb_grid, points_distance), offsetof(pgb_grid, clip), offsetof(pgb_grid, mode));\n"
         'printf("%zu %zu %zu %zu\\n", sizeof(pgb_cameras), offsetof(pgb_cameras, camera_angle_x),'
         " offsetof(pgb_cameras, near), offsetof(pgb_cameras, seed));\n"
-        'printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(pgb_rays), offsetof(pgb_rays, num_rays),'
+        'printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(pgb_rays), offsetof(pgb_rays, num_rays),'
         " offsetof(pgb_rays, delta_step), offsetof(pgb_rays, seed), offsetof(pgb_rays, term_threshold),"
-        " offsetof(pgb_rays, background), offsetof(pgb_rays, log_transmittance));\n"
+        " offsetof(pgb_rays, background), offsetof(pgb_rays, log_transmittance),"
+        " offsetof(pgb_rays, chunk_samples));\n"
         'printf("%zu %zu %zu %zu %zu\\n", sizeof(pgb_scene), offsetof(pgb_scene, dims),'
         " offsetof(pgb_scene, origin), offsetof(pgb_scene, num_samples), offsetof(pgb_scene, delta_step));\n"
         "return 0;}\n")
@@ -56,7 +57,8 @@ def test_struct_layout_matches_header(tmp_path):
     assert g == [ctypes.sizeof(G), G.origin.offset, G.points_distance.offset, G.clip.offset, G.mode.offset]
     assert c == [ctypes.sizeof(C), C.camera_angle_x.offset, C.near.offset, C.seed.offset]
     assert r == [ctypes.sizeof(R), R.num_rays.offset, R.delta_step.offset, R.seed.offset,
-                 R.term_threshold.offset, R.background.offset, R.log_transmittance.offset]
+                 R.term_threshold.offset, R.background.offset, R.log_transmittance.offset,
+                 R.chunk_samples.offset]
     sc = list(map(int, out[3].split()))
     P = _lib.PgbScene
     assert sc == [ctypes.sizeof(P), P.dims.offset, P.origin.offset, P.num_samples.offset,
@@ -122,10 +124,6 @@ def test_argument_validation_without_launch(lib):
                                 None) == _lib.PGB_ERR_ARG
     assert lib.pgb_wrap_indices(None, 3, None, None) == _lib.PGB_ERR_ARG
     assert lib.pgb_fill_zero(24, 16, None) == _lib.PGB_ERR_ALIGN
-    assert lib.pgb_probe_random_reads(None, 256, 8, 1, 16, None) == _lib.PGB_ERR_ARG
-    assert lib.pgb_probe_random_reads(24, 256, 8, 1, 16, None) == _lib.PGB_ERR_ALIGN
-    assert lib.pgb_probe_random_atomics(16, 8, 8, 1, None) == _lib.PGB_ERR_ARG  # < one slot
-    assert lib.pgb_probe_random_atomics(16, 256, 0, 1, None) == _lib.PGB_OK  # nothing to do
     # even_spread with a non-square ray count
     assert lib.pgb_generate_rays(16, 1, 10, ctypes.c_float(0.5), 16, 4, 4, None, 1, 16, 16, None,
                                  None) == _lib.PGB_ERR_ARG
@@ -144,3 +142,15 @@ def test_operators_reject_cpu_tensors():
         pg.generate_grid(4, 4, 4, device="cpu")
     with pytest.raises(ValueError):
         pg.compute_alpha_weighted_pixels(torch.zeros(1, 2, 3, 4))
+
+
+def test_probe_helper_loads_and_validates_arguments():
+    """The device-memory probes live in their own helper library (not the renderer's ABI):
+    it loads and rejects bad arguments without launching anything."""
+    from plenoxels_gb300 import probes
+    p = probes.load()
+    assert p.pgb_probe_random_reads(None, 256, 8, 1, 16, None) == _lib.PGB_ERR_ARG
+    assert p.pgb_probe_random_reads(24, 256, 8, 1, 16, None) == _lib.PGB_ERR_ALIGN
+    assert p.pgb_probe_random_atomics(16, 8, 8, 1, None) == _lib.PGB_ERR_ARG  # < one slot
+    assert p.pgb_probe_random_atomics(16, 256, 0, 1, None) == _lib.PGB_OK  # nothing to do
+    assert not any(n.startswith("pgb_probe") for n in _declared())
