@@ -80,6 +80,15 @@ typedef struct {
   int32_t log_transmittance; /* 1: T = exp(compensated sum of log(1 - alpha)) instead of the
                                 reference's product; fp32/BF16 grids with clip only (the
                                 precision form; no counterpart in the reference) */
+  int32_t chunk_samples;    /* samples a warp gathers between transmittance checks: 0 picks
+                               automatically, else 32, 64, 128, 256 or 512 (raised when a ray
+                               would span more than 32 chunks). With clip on (and no beta
+                               term), a ray stops after the chunk in which its transmittance
+                               reaches exactly 0, once the samples behind the opaque sample
+                               can no longer change a gradient (its own alpha gradient is
+                               masked by the clamp, or a second opaque sample was read):
+                               results are unchanged and the rest of the ray is never read.
+                               Tuning only. */
 } pgb_rays;
 
 /* ---- fused render path (scripts/train.py:142-156 composed with src/ray_sampling.py,
@@ -144,6 +153,11 @@ int pgb_render_train_terms(const pgb_grid* grid, const pgb_rays* rays, const voi
  * [R,S]. index_out is int64. */
 int pgb_render_sample_indices(const pgb_grid* grid, const pgb_rays* rays, int64_t* index_out,
                               uint8_t* inbounds_out, pgb_stream_t stream);
+/* The normalised coordinates (position - origin) / points_distance of every sample of
+ * every ray, as the fused kernels compute them (src/ray_sampling.py:161-167, :12-13):
+ * coords_out [R,S,3] Real. */
+int pgb_render_sample_coords(const pgb_grid* grid, const pgb_rays* rays, void* coords_out,
+                             pgb_stream_t stream);
 
 /* ---- batched form: many scenes, one persistent launch per training step ----
  * Scenes of different sizes, each a dense [X,Y,Z,4] grid (BF16 or fp32 cells) whose
@@ -193,15 +207,17 @@ int pgb_batch_zero_grads(const pgb_scene* scenes, int32_t num_scenes, int64_t ma
  * 32*slots_per_lane samples). slots_per_lane in {1,2,4,8} and threads_per_block in
  * {128,256} are the tile choices (0: defaults); a ray spans at most 32 chunks, so every
  * scene needs num_samples <= 1024 * slots_per_lane (a longer ray's loss and RGBA come
- * back NaN). workspace: pgb_batch_workspace_bytes(R),
- * zeroed once before first use; the kernel leaves its counters zeroed. */
+ * back NaN). merge_updates = 1 (trilinear) sums the updates that lanes of a warp make to
+ * the same cell before the atomic adds (a tile choice: same gradient, summed in another
+ * order). workspace: pgb_batch_workspace_bytes(R), zeroed once before first use; the
+ * kernel leaves its counters zeroed. */
 int64_t pgb_batch_workspace_bytes(int64_t num_rays);
 int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, int32_t mode,
                     int32_t clip, const float* origins, const float* dirs, const float* target,
                     const int32_t* ray_scene, int64_t num_rays, float term_threshold,
                     int32_t stratified, uint64_t seed, double loss_weight, float* rgba_out,
                     float* loss_out, void* workspace, int32_t slots_per_lane,
-                    int32_t threads_per_block, pgb_stream_t stream);
+                    int32_t threads_per_block, int32_t merge_updates, pgb_stream_t stream);
 
 /* ---- optimiser side of the training step (scripts/train.py:44-65, :89, :163-184) ---- */
 
@@ -364,17 +380,6 @@ int pgb_splat_preview(const float* cells, const int32_t dims[3], float points_di
  * cleared. kernel_size odd and <= 7; sums_scratch holds X*Y*Z floats. */
 int pgb_remove_noise(float* cells, const int32_t dims[3], int32_t kernel_size, double radius,
                      float threshold, int32_t repeats, float* sums_scratch, pgb_stream_t stream);
-
-/* Device-memory probes (no counterpart in the reference): num_reads independent 16 B
- * loads, or num_updates float4 atomic adds of 1, at pseudo-random 16 B slots of a
- * 16-byte-aligned device buffer of table_bytes bytes (every slot inside it). Timed by the
- * caller around the launch, they give the random 32 B sector rate that bounds the render
- * kernels' cell gathers and gradient scatters. sink: one device float, written only if
- * the loaded values sum to -1. */
-int pgb_probe_random_reads(const void* table, int64_t table_bytes, int64_t num_reads, uint64_t seed,
-                           float* sink, pgb_stream_t stream);
-int pgb_probe_random_atomics(void* table, int64_t table_bytes, int64_t num_updates, uint64_t seed,
-                             pgb_stream_t stream);
 
 /* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel: the
  * gradient zeroing of optimizer.zero_grad() (scripts/train.py:180) and of a fresh .grad. */

@@ -12,7 +12,9 @@ from ctypes import (POINTER, Structure, c_char_p, c_double, c_float, c_int32, c_
 
 import torch
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libplenoxels_gb300.so")
+# PLENOXELS_GB300_LIB names an alternative build (plenoxels_gb300.build with lib_path)
+LIB_PATH = os.environ.get("PLENOXELS_GB300_LIB") or os.path.join(
+    os.path.dirname(os.path.abspath(__file__)), "libplenoxels_gb300.so")
 
 PGB_OK, PGB_ERR_ARG, PGB_ERR_ALIGN, PGB_ERR_LAUNCH, PGB_ERR_UNSUPPORTED = 0, -1, -2, -3, -4
 PGB_F32, PGB_BF16, PGB_F64 = 0, 1, 2
@@ -61,6 +63,7 @@ class PgbRays(Structure):
         ("use_background", c_int32),
         ("background", c_float * 3),
         ("log_transmittance", c_int32),
+        ("chunk_samples", c_int32),
     ]
 
 
@@ -93,12 +96,13 @@ _SIGNATURES = {
     "pgb_render_train_terms": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, POINTER(PgbLossTerms), _P, _P, _P, _P, _P]),
     "pgb_render_train_noalloc": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, c_double, _P, _P, _P, _P]),
     "pgb_render_sample_indices": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P, _P]),
+    "pgb_render_sample_coords": (c_int32, [POINTER(PgbGrid), POINTER(PgbRays), _P, _P]),
     "pgb_build_bricks": (c_int32, [_P, POINTER(c_int32), c_int32, _P, _P]),
     "pgb_pack_mask": (c_int32, [_P, c_int64, _P, _P]),
     "pgb_batch_zero_grads": (c_int32, [_P, c_int32, c_int64, _P]),
     "pgb_batch_workspace_bytes": (c_int64, [c_int64]),
     "pgb_batch_train": (c_int32, [_P, c_int32, c_int32, c_int32, c_int32, _P, _P, _P, _P, c_int64, c_float,
-                                  c_int32, c_uint64, c_double, _P, _P, _P, c_int32, c_int32, _P]),
+                                  c_int32, c_uint64, c_double, _P, _P, _P, c_int32, c_int32, c_int32, _P]),
     "pgb_tv_workspace_bytes": (c_int64, []),
     "pgb_tv_sumsq": (c_int32, [_P, POINTER(c_int32), _P, _P, _P]),
     "pgb_tv_grad": (c_int32, [_P, POINTER(c_int32), _P, c_float, _P, _P]),
@@ -126,8 +130,6 @@ _SIGNATURES = {
     "pgb_composite_fwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P]),
     "pgb_composite_bwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P, _P]),
     "pgb_fill_zero": (c_int32, [_P, c_int64, _P]),
-    "pgb_probe_random_reads": (c_int32, [_P, c_int64, c_int64, c_uint64, _P, _P]),
-    "pgb_probe_random_atomics": (c_int32, [_P, c_int64, c_int64, c_uint64, _P]),
     "pgb_rgba_to_image": (c_int32, [_P, c_int32, _P, _P]),
     "pgb_splat_size": (c_int32, [POINTER(c_float), c_int32, POINTER(c_int32)]),
     "pgb_splat_preview": (c_int32, [_P, POINTER(c_int32), c_float, POINTER(c_float), c_float, c_int32, c_float,

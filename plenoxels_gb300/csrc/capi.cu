@@ -5,7 +5,7 @@
 #include <cmath>
 
 #include "pgb_host.h"
-#include "render.cuh"
+#include "render_args.cuh"
 
 namespace pgb {
 
@@ -42,107 +42,12 @@ int op_composite(const void*, int, int64_t, int, const void*, void*, int, cudaSt
 int composite_max_samples();
 int op_render_indices_f32(const RenderArgs<float>&, int, int64_t*, uint8_t*, cudaStream_t);
 int op_render_indices_f64(const RenderArgs<double>&, int, int64_t*, uint8_t*, cudaStream_t);
+int op_render_coords_f32(const RenderArgs<float>&, float*, cudaStream_t);
+int op_render_coords_f64(const RenderArgs<double>&, double*, cudaStream_t);
 int op_fill_zero(void*, int64_t, cudaStream_t);
 int op_rgba_to_image(const float*, int, uint8_t*, cudaStream_t);
 
 namespace {
-
-inline bool aligned(const void* p, uintptr_t a) { return ((uintptr_t)p % a) == 0; }
-
-int check_grid(const pgb_grid* g) {
-  if (!g || !g->cells) return PGB_ERR_ARG;
-  if (g->dtype != PGB_F32 && g->dtype != PGB_BF16 && g->dtype != PGB_F64) return PGB_ERR_ARG;
-  if (g->mode != PGB_NEAREST && g->mode != PGB_TRILINEAR) return PGB_ERR_ARG;
-  for (int a = 0; a < 3; ++a)
-    if (g->dims[a] <= 0) return PGB_ERR_ARG;
-  const uint64_t cells = (uint64_t)g->dims[0] * g->dims[1] * g->dims[2];
-  if (cells >= (1ull << 40)) return PGB_ERR_UNSUPPORTED;
-  if (!aligned(g->cells, g->dtype == PGB_BF16 ? 8 : 16)) return PGB_ERR_ALIGN;
-  return PGB_OK;
-}
-
-template <typename Real>
-GridP<Real> grid_params(const pgb_grid* g) {
-  GridP<Real> p = {};
-  p.cells = g->cells;
-  p.X = g->dims[0]; p.Y = g->dims[1]; p.Z = g->dims[2];
-  p.fX = (Real)p.X; p.fY = (Real)p.Y; p.fZ = (Real)p.Z;
-  p.ox = (Real)g->origin[0]; p.oy = (Real)g->origin[1]; p.oz = (Real)g->origin[2];
-  p.pd = (Real)g->points_distance;
-  p.clip = g->clip ? 1 : 0;
-  p.alpha_floor = g->alpha_floor;
-  return p;
-}
-
-int check_rays(const pgb_grid* g, const pgb_rays* r, bool need_target_or_cams) {
-  if (!r || r->num_rays < 0 || r->num_samples < 0) return PGB_ERR_ARG;
-  if (r->num_samples > kMaxSamples) return PGB_ERR_UNSUPPORTED;
-  if (r->log_transmittance) {
-    if (g->dtype == PGB_F64) return PGB_ERR_UNSUPPORTED;
-    if (!g->clip) return PGB_ERR_ARG;  // log(1 - alpha) needs alpha in [0, 1]
-  }
-  if (r->cameras) {
-    const pgb_cameras* c = r->cameras;
-    if (g->dtype == PGB_F64) return PGB_ERR_UNSUPPORTED;
-    if (!c->transforms || !c->images || c->num_cameras <= 0 || c->height <= 0 || c->width <= 0)
-      return PGB_ERR_ARG;
-    if (c->height != c->width) return PGB_ERR_UNSUPPORTED;
-    if (!aligned(c->images, 16)) return PGB_ERR_ALIGN;
-  } else if (r->num_rays > 0 && (!r->origins || !r->dirs)) {
-    return PGB_ERR_ARG;
-  }
-  (void)need_target_or_cams;
-  return PGB_OK;
-}
-
-template <typename Real>
-RenderArgs<Real> render_args(const pgb_grid* g, const pgb_rays* r) {
-  RenderArgs<Real> a = {};
-  a.g = grid_params<Real>(g);
-  a.origins = (const Real*)r->origins;
-  a.dirs = (const Real*)r->dirs;
-  if (r->cameras) {
-    const pgb_cameras* c = r->cameras;
-    a.use_cameras = 1;
-    a.transforms = c->transforms;
-    a.images = c->images;
-    a.C = c->num_cameras;
-    a.H = c->height;
-    a.W = c->width;
-    a.fov = c->camera_angle_x;
-    a.near_dist = c->near;
-    a.cam_seed = c->seed;
-  }
-  a.R = r->num_rays;
-  a.S = r->num_samples;
-  a.delta = (Real)r->delta_step;
-  a.stratified = r->stratified ? 1 : 0;
-  a.strat_seed = r->seed;
-  a.term_thr = r->term_threshold;
-  a.use_bg = r->use_background ? 1 : 0;
-  for (int c = 0; c < 3; ++c) a.bg[c] = r->background[c];
-  return a;
-}
-
-template <typename Real>
-int dispatch_render(const pgb_grid* g, const pgb_rays* r, RenderArgs<Real>& a, int phase,
-                    cudaStream_t s);
-
-template <>
-int dispatch_render<float>(const pgb_grid* g, const pgb_rays* r, RenderArgs<float>& a, int phase,
-                           cudaStream_t s) {
-  if (r->log_transmittance)
-    return g->dtype == PGB_BF16 ? launch_render_logt_bf16(a, g->mode, phase, s)
-                                : launch_render_logt_f32(a, g->mode, phase, s);
-  return g->dtype == PGB_BF16 ? launch_render_bf16(a, g->mode, phase, s)
-                              : launch_render_f32(a, g->mode, phase, s);
-}
-template <>
-int dispatch_render<double>(const pgb_grid* g, const pgb_rays* r, RenderArgs<double>& a, int phase,
-                            cudaStream_t s) {
-  (void)r;  // check_rays rejects the log-sum form for fp64 grids
-  return launch_render_f64(a, g->mode, phase, s);
-}
 
 template <typename Real>
 int render_common(const pgb_grid* g, const pgb_rays* r, int phase, void* rgba_out,
@@ -256,6 +161,18 @@ int pgb_render_sample_indices(const pgb_grid* grid, const pgb_rays* rays, int64_
   }
   RenderArgs<float> a = render_args<float>(grid, rays);
   return op_render_indices_f32(a, grid->mode, index_out, inbounds_out, stream);
+}
+
+int pgb_render_sample_coords(const pgb_grid* grid, const pgb_rays* rays, void* coords_out,
+                             pgb_stream_t stream) {
+  int st = check_grid(grid);
+  if (st) return st;
+  if ((st = check_rays(grid, rays, false))) return st;
+  if (rays->num_rays == 0 || rays->num_samples == 0) return PGB_OK;
+  if (!coords_out) return PGB_ERR_ARG;
+  if (grid->dtype == PGB_F64)
+    return op_render_coords_f64(render_args<double>(grid, rays), (double*)coords_out, stream);
+  return op_render_coords_f32(render_args<float>(grid, rays), (float*)coords_out, stream);
 }
 
 int pgb_generate_rays(const float* transforms, int32_t num_cameras, int64_t rays_per_camera,

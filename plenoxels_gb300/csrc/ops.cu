@@ -769,6 +769,33 @@ int op_composite(const void* samples, int f64, int64_t M, int S, const void* dou
 }
 int composite_max_samples() { return kMaxChunks * kWarp * kCompK; }
 
+// Normalised coordinates (p - origin) / pd of every sample of every ray, as the fused
+// kernels compute them: out[(r * S + s) * 3 + axis].
+template <typename Real>
+__global__ void render_coords_kernel(const RenderArgs<Real> a, Real* __restrict__ out) {
+  const int64_t total = a.R * (int64_t)a.S;
+  PGB_FOR(i, total) {
+    const int64_t r = i / a.S;
+    const int s = (int)(i - r * a.S);
+    Ray<Real> ray;
+    load_ray(a, r, ray, false);
+    Real nx, ny, nz;
+    sample_coords(a, ray, s, nx, ny, nz);
+    out[3 * i + 0] = nx;
+    out[3 * i + 1] = ny;
+    out[3 * i + 2] = nz;
+  }
+}
+
+int op_render_coords_f32(const RenderArgs<float>& a, float* out, cudaStream_t s) {
+  render_coords_kernel<float><<<blocks_for(a.R * (int64_t)a.S), kThreads, 0, s>>>(a, out);
+  return after_launch();
+}
+int op_render_coords_f64(const RenderArgs<double>& a, double* out, cudaStream_t s) {
+  render_coords_kernel<double><<<blocks_for(a.R * (int64_t)a.S), kThreads, 0, s>>>(a, out);
+  return after_launch();
+}
+
 template <typename Real>
 static int render_indices_t(const RenderArgs<Real>& a, int mode, int64_t* idx, uint8_t* inb,
                             cudaStream_t s) {

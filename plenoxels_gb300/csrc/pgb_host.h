@@ -28,12 +28,26 @@ int launch_render_f64(const RenderArgs<double>& a, int mode, int phase, cudaStre
 int launch_render_logt_f32(const RenderArgs<float>& a, int mode, int phase, cudaStream_t s);
 int launch_render_logt_bf16(const RenderArgs<float>& a, int mode, int phase, cudaStream_t s);
 
-// Slots per lane (K) used for a ray of S samples: one chunk up to 512 samples,
-// 256-sample chunks beyond.
-inline int pick_slots(int S) {
+// Slots per lane (K) of a chunk of 32 * K samples. A requested chunk size (32 * K for K
+// in 1, 2, 4, 8, 16) is raised until a ray spans at most kMaxChunks chunks. Without one:
+// when rays can stop at the first chunk whose transmittance reaches 0 (clip on, no beta
+// term), short chunks (32 samples for trilinear lookup, 64 for nearest) skip the most
+// samples behind opaque cells (measured on GB300: 256^3 grid, 8192 rays x 256 samples,
+// trilinear step 0.175 ms with one 256-sample chunk, 0.133 ms with 32-sample chunks);
+// otherwise a ray up to 512 samples is a single chunk and longer rays use 256-sample
+// chunks.
+inline int pick_slots(int S, int chunk_samples = 0, bool early_stop = false,
+                      int mode = PGB_TRILINEAR) {
 #ifdef PGB_FORCE_SLOTS
   if (S <= 32 * kMaxChunks * PGB_FORCE_SLOTS) return PGB_FORCE_SLOTS;
 #endif
+  if (chunk_samples <= 0 && early_stop) chunk_samples = mode == PGB_NEAREST ? 64 : 32;
+  if (chunk_samples > 0) {
+    int k = 1;
+    while (k < 16 && 32 * k < chunk_samples) k *= 2;
+    while (k < 16 && (S + 32 * k - 1) / (32 * k) > kMaxChunks) k *= 2;
+    return k;
+  }
   if (S <= 64) return 2;
   if (S <= 128) return 4;
   if (S <= 256) return 8;

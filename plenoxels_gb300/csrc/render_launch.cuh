@@ -37,7 +37,9 @@ int launch_render_k(const RenderArgs<Real>& a, cudaStream_t s) {
 
 template <typename Real, typename Store, int MODE, int PHASE, bool LOGT>
 int launch_render_mp(const RenderArgs<Real>& a, cudaStream_t s) {
-  switch (pick_slots(a.S)) {
+  const bool early_stop = a.g.clip && !(PHASE == kTrain && a.beta_w != 0.0);
+  switch (pick_slots(a.S, a.chunk_samples, early_stop, MODE)) {
+    case 1: return launch_render_k<Real, Store, MODE, 1, PHASE, LOGT>(a, s);
     case 2: return launch_render_k<Real, Store, MODE, 2, PHASE, LOGT>(a, s);
     case 4: return launch_render_k<Real, Store, MODE, 4, PHASE, LOGT>(a, s);
     case 8: return launch_render_k<Real, Store, MODE, 8, PHASE, LOGT>(a, s);

@@ -36,7 +36,7 @@ def _transmittance(name: str) -> int:
 
 
 def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, seed, term_threshold,
-               cameras=None, background=None, log_t=0) -> PgbRays:
+               cameras=None, background=None, log_t=0, chunk_samples=0) -> PgbRays:
     r = PgbRays()
     r.origins = ptr(origins)
     r.dirs = ptr(dirs)
@@ -51,6 +51,7 @@ def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, see
         r.use_background = 1
         r.background[:] = [float(v) for v in background]
     r.log_transmittance = int(log_t)
+    r.chunk_samples = int(chunk_samples)
     return r
 
 
@@ -74,7 +75,8 @@ class _RenderRays(torch.autograd.Function):
         gdesc = _lib.make_grid(grid, cfg["origin"], cfg["points_distance"], cfg["mode"], cfg["clip"])
         rdesc = _rays_desc(origins, dirs, R, cfg["num_samples"], cfg["delta_step"],
                            cfg["stratified"], cfg["seed"], cfg["term_threshold"],
-                           background=cfg["background"], log_t=cfg["log_t"])
+                           background=cfg["background"], log_t=cfg["log_t"],
+                           chunk_samples=cfg["chunk_samples"])
         check(lib.pgb_render_fwd(gdesc, rdesc, ptr(rgba), stream_of(grid)), "render_rays")
         ctx.save_for_backward(grid, origins, dirs)
         ctx.cfg = cfg
@@ -92,14 +94,15 @@ class _RenderRays(torch.autograd.Function):
         gdesc = _lib.make_grid(grid, cfg["origin"], cfg["points_distance"], cfg["mode"], cfg["clip"])
         rdesc = _rays_desc(origins, dirs, origins.shape[0], cfg["num_samples"], cfg["delta_step"],
                            cfg["stratified"], cfg["seed"], cfg["term_threshold"],
-                           background=cfg["background"], log_t=cfg["log_t"])
+                           background=cfg["background"], log_t=cfg["log_t"],
+                           chunk_samples=cfg["chunk_samples"])
         check(lib.pgb_render_bwd(gdesc, rdesc, ptr(d_rgba), ptr(grad), s), "render_rays backward")
         return grad, None, None, None
 
 
 def render_rays(grid, origins, dirs, delta_step, num_samples, points_distance, grid_min=None,
                 mode="trilinear", clip=True, stratified=False, seed=0, term_threshold=0.0,
-                background=None, transmittance="product"):
+                background=None, transmittance="product", chunk_samples=0):
     """Premultiplied RGBA [R,4] of rays through a dense [X,Y,Z,4] grid.
 
     Samples sit at origins + dirs * (delta_step * k), k = 1..num_samples (minus a
@@ -107,7 +110,9 @@ def render_rays(grid, origins, dirs, delta_step, num_samples, points_distance, g
     (0,0,0) (default: generate_grid's layout, grid_origin()). background (3 values, e.g. white)
     composites rgb over it: rgb + (1 - alpha) * background. transmittance "logsum" evaluates
     T = exp(compensated sum of log(1 - alpha)) instead of the reference's running product
-    (fp32/BF16 grids, clip=True). Differentiable in grid."""
+    (fp32/BF16 grids, clip=True). chunk_samples (0: automatic; 32..512) sets how many
+    samples of a ray are gathered between transmittance checks; it changes speed only.
+    Differentiable in grid."""
     require_cuda(grid, origins, dirs)
     _check_rays(grid, origins, dirs)
     if grid_min is None:
@@ -117,7 +122,7 @@ def render_rays(grid, origins, dirs, delta_step, num_samples, points_distance, g
                delta_step=float(delta_step), stratified=bool(stratified), seed=int(seed),
                term_threshold=float(term_threshold),
                background=None if background is None else tuple(float(v) for v in background),
-               log_t=_transmittance(transmittance))
+               log_t=_transmittance(transmittance), chunk_samples=int(chunk_samples))
     return _RenderRays.apply(grid.contiguous(), origins.contiguous(), dirs.contiguous(), cfg)
 
 
@@ -162,9 +167,10 @@ def _camera_desc(transforms, images, camera_angle_x, ray_seed, near) -> PgbCamer
 
 def camera_sample_indices(grid, transforms, images, camera_angle_x, num_rays, ray_seed, near,
                           delta_step, num_samples, points_distance, grid_min=None,
-                          mode="trilinear", stratified=False, seed=0):
+                          mode="trilinear", stratified=False, seed=0, return_coords=False):
     """render_sample_indices for rays generated in-kernel from cameras (the rays
-    FusedTrainStep.step_cameras uses for the same arguments)."""
+    FusedTrainStep.step_cameras uses for the same arguments). return_coords=True adds the
+    samples' normalised coordinates [R,S,3] as a third result."""
     require_cuda(grid)
     if grid_min is None:
         grid_min = grid_origin(grid.shape, points_distance, _lib.real_dtype(grid.dtype))
@@ -178,7 +184,12 @@ def camera_sample_indices(grid, transforms, images, camera_angle_x, num_rays, ra
     rdesc = _rays_desc(None, None, R, S, delta_step, stratified, seed, 0.0, cameras=cams)
     check(_lib.load().pgb_render_sample_indices(gdesc, rdesc, ptr(idx), ptr(inb), stream_of(grid)),
           "camera_sample_indices")
-    return idx, inb
+    if not return_coords:
+        return idx, inb
+    coords = torch.empty(R, S, 3, dtype=_lib.real_dtype(grid.dtype), device=grid.device)
+    check(_lib.load().pgb_render_sample_coords(gdesc, rdesc, ptr(coords), stream_of(grid)),
+          "camera_sample_indices")
+    return idx, inb, coords
 
 
 class FusedTrainStep:
@@ -187,6 +198,7 @@ class FusedTrainStep:
     beta > 0 adds the reference's beta loss on the sampled opacities (scripts/train.py:
     170-177) in the same launch; ``self.losses`` holds [weighted MSE, beta term].
     transmittance="logsum" selects the compensated log-sum transmittance (see render_rays).
+    chunk_samples as in render_rays (speed only).
 
     The gradient goes to ``self.grad`` (fp32 for fp32/bf16 grids, fp64 for fp64 grids),
     which is also attached as ``grid.grad`` when the dtypes agree, so a torch optimizer
@@ -203,7 +215,7 @@ class FusedTrainStep:
     def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
                  grid_min=None, clip=True, stratified=False, seed=0, term_threshold=0.0,
                  loss_weight=1.0, overlap_zero=False, beta=0.0, beta_eps=1e-4, background=None,
-                 transmittance="product"):
+                 transmittance="product", chunk_samples=0):
         require_cuda(grid)
         if grid.dim() != 4 or grid.shape[-1] != 4 or not grid.is_contiguous():
             raise ValueError("grid must be a contiguous [X,Y,Z,4] tensor")
@@ -224,6 +236,7 @@ class FusedTrainStep:
         self.beta_eps = float(beta_eps)
         self.background = None if background is None else tuple(float(v) for v in background)
         self.log_t = _transmittance(transmittance)
+        self.chunk_samples = int(chunk_samples)
         lib = _lib.load()
         dev = grid.device
         self.workspace = torch.zeros(lib.pgb_train_workspace_bytes(), dtype=torch.uint8, device=dev)
@@ -309,7 +322,7 @@ class FusedTrainStep:
             raise ValueError(f"target must be [R,4] {self.real}")
         rdesc = _rays_desc(origins, dirs, origins.shape[0], self.num_samples, self.delta_step,
                            self.stratified, self.seed, self.term_threshold, background=self.background,
-                           log_t=self.log_t)
+                           log_t=self.log_t, chunk_samples=self.chunk_samples)
         return self._launch(rdesc, target.contiguous(), rgba_out, zero_grad)
 
     def step_cameras(self, transforms, images, camera_angle_x, num_rays, ray_seed, near=0.0,
@@ -321,5 +334,5 @@ class FusedTrainStep:
         self._cams = cams  # keep alive for the call
         rdesc = _rays_desc(None, None, num_rays, self.num_samples, self.delta_step, self.stratified,
                            self.seed, self.term_threshold, cameras=cams, background=self.background,
-                           log_t=self.log_t)
+                           log_t=self.log_t, chunk_samples=self.chunk_samples)
         return self._launch(rdesc, None, rgba_out, zero_grad)

@@ -225,7 +225,8 @@ def test_overlapped_gradient_zeroing_gives_the_same_steps():
 def test_random_access_probes_stay_inside_their_table():
     """The memory probes behind the roofline report: every atomic lands in the table
     (its sum is exactly 4 per update) and the read probe completes."""
-    lib = _lib.load()
+    from plenoxels_gb300 import probes
+    lib = probes.load()
     stream = torch.cuda.current_stream().cuda_stream
     table = torch.zeros(1000 * 4, device=DEV)  # 1000 slots of 16 B
     n = 123457
@@ -355,3 +356,36 @@ def test_rays_clipped_to_the_grid_match_oracle(mode):
     target = torch.rand(o.shape[0], 4, generator=g)
     _parity(grid, o, d, target, 1200, 12.0 / 1200, pd, gmin, mode, strat=True)
     _parity(grid, o, d, target, 96, 0.06, pd, gmin, mode)
+
+
+@pytest.mark.parametrize("mode", ["nearest", "trilinear"])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_early_stop_behind_opaque_cells_is_exact(mode, dtype):
+    """Rays stop after the chunk where their transmittance reaches 0. The first opaque
+    sample's own alpha gradient reads the samples behind it when the clamp passes it (a
+    stored alpha of exactly 1.0), so every chunk size must give the oracle's loss and
+    gradient, on a grid where opaque cells hold exactly 1.0 or values above 1."""
+    side, S, R = 32, 256, 600
+    g = scenes.make_grid(side, 5, 201, amp=(0.8, 6.0))
+    rng = np.random.default_rng(202)
+    a = g[..., 3]
+    opaque = a >= 1.0
+    a[opaque & (rng.random(a.shape) < 0.5)] = 1.0  # clamp gradient open at exactly 1
+    a[(a > 0.9) & (a < 1.0)] = 1.0
+    grid = torch.from_numpy(g).to(dtype).float()  # the values the kernels see
+    assert int((grid[..., 3] == 1.0).sum()) > 100 and int((grid[..., 3] > 1.0).sum()) > 100
+    T = torch.from_numpy(scenes.make_cameras(4, 203))
+    imgs = torch.from_numpy(scenes.make_images(4, 16, 16, 204))
+    o, d, tgt = tp.camera_batch(T, 0.691, imgs, R, 205, 2.0)
+    pd, delta = scenes.points_distance(side), 4.0 / S
+    ref = grid.clone().requires_grad_(True)
+    loss = tp.train_loss(ref, o, d, tgt, S, delta, tp.grid_min(grid.shape, pd), pd, mode)
+    loss.backward()
+    for chunk in (32, 64, 128, 256):
+        step = pg.FusedTrainStep(grid.to(dtype).to(DEV), pd, S, delta, mode=mode,
+                                 chunk_samples=chunk)
+        rgba = torch.empty(R, 4, device=DEV)
+        got = step.step_rays(o.to(DEV), d.to(DEV), tgt.to(DEV), rgba_out=rgba)
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(float(got), float(loss), rtol=1e-5, err_msg=f"chunk {chunk}")
+        _grad_close(step.grad, ref.grad)
