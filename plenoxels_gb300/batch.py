@@ -80,7 +80,10 @@ class Scene:
         return desc
 
 
-TILE_CANDIDATES = [(1, 256), (2, 256), (2, 128), (4, 256), (4, 128), (8, 256)]
+# (samples per lane K, threads per block, merge): merge = 1 sums a warp's updates of the
+# same cell before the atomics (trilinear)
+TILE_CANDIDATES = [(1, 256, 0), (1, 256, 1), (2, 256, 0), (2, 256, 1), (2, 128, 0), (4, 256, 0),
+                   (4, 128, 0), (8, 256, 0)]
 
 
 class BatchedTrainStep:
@@ -107,8 +110,8 @@ class BatchedTrainStep:
         self.loss_weight = float(loss_weight)
         self.max_samples = max(int(sc.num_samples) for sc in scenes)
         if tiles is None:
-            tiles = (next((k for k in (2, 4, 8) if 32 * 32 * k >= self.max_samples), 8), 256)
-        self.tiles = tuple(tiles)
+            tiles = (next((k for k in (2, 4, 8) if 32 * 32 * k >= self.max_samples), 8), 256, 0)
+        self.tiles = self._tile(tiles)
         dev = scenes[0].cells.device
         self.device = dev
         if self.max_samples > 32 * 32 * 8:
@@ -130,6 +133,12 @@ class BatchedTrainStep:
         self.loss = torch.zeros((), device=dev)
         self.rgba = None
         self.graph = None
+
+    @staticmethod
+    def _tile(tile):
+        """(K, threads, merge) from a 2- or 3-tuple (merge defaults to 0)."""
+        t = tuple(int(v) for v in tile)
+        return t if len(t) == 3 else (t[0], t[1], 0)
 
     def _tile_fits(self, tile):
         # a ray spans at most 32 chunks of 32 * K samples
@@ -162,13 +171,13 @@ class BatchedTrainStep:
         s = torch.cuda.current_stream(self.device).cuda_stream
         check(lib.pgb_batch_zero_grads(ptr(self.scene_table), len(self.scenes), self.max_cells, s),
               "batched step")
-        K, threads = tiles or self.tiles
+        K, threads, merge = self._tile(tiles or self.tiles)
         check(lib.pgb_batch_train(ptr(self.scene_table), len(self.scenes), self.dtype, self.mode,
                                   1 if self.clip else 0, ptr(self.origins), ptr(self.dirs),
                                   ptr(self.target), ptr(self.ray_scene), self.num_rays,
                                   self.term_threshold, 1 if self.stratified else 0, self.seed,
                                   self.loss_weight, ptr(self.rgba), ptr(self.loss),
-                                  ptr(self.workspace), K, threads, s), "batched step")
+                                  ptr(self.workspace), K, threads, merge, s), "batched step")
         return self.loss
 
     def step(self):
@@ -194,7 +203,7 @@ class BatchedTrainStep:
         return g
 
     def autotune(self, candidates=TILE_CANDIDATES, reps=5, brick_sizes=None):
-        """Times each (samples-per-lane, threads-per-block) tile on the current rays, for
+        """Times each (samples-per-lane, threads-per-block, merge) tile on the current rays, for
         each empty-space brick size 2^L in brick_sizes (default: the current one), and keeps
         the fastest; returns {tile: ms} at the chosen brick size (self.brick_log2)."""
         if self.graph is not None:
@@ -203,7 +212,7 @@ class BatchedTrainStep:
         for L in (brick_sizes or (self.brick_log2,)):
             self._set_bricks(L)
             times = {}
-            for tile in (t for t in candidates if self._tile_fits(t)):
+            for tile in (self._tile(t) for t in candidates if self._tile_fits(t)):
                 self._run(tile)
                 torch.cuda.synchronize(self.device)
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -134,7 +134,9 @@ PGB_BATCH_GATHER_ATTR bool batch_sample(const RenderArgs<float>& ra, const Ray<f
   return true;
 }
 
-template <typename Store, int MODE, int K>
+// MERGE: the trilinear scatter merges the warp's updates of the same cell
+// (warp_merged_scatter) before its atomics.
+template <typename Store, int MODE, int K, bool MERGE>
 __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCKS_K1 : PGB_BATCH_MIN_BLOCKS)
     batch_train_kernel(const BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -290,7 +292,19 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
         float S_after = __shfl_down_sync(kFull, S_here, 1);
         if (lane == kWarp - 1) S_after = Snext_carry;
         Snext_carry = __shfl_sync(kFull, S_here, 0);
-        if (bk != 0u) {
+        if (MERGE && MODE == PGB_TRILINEAR) {
+          float dv[4] = {0.f, 0.f, 0.f, 0.f};
+          float nx = 0.f, ny = 0.f, nz = 0.f;
+          bool has = false;
+          if (bk != 0u) {
+            const float w = al * tk;
+            dv[0] = gpx[0] * w; dv[1] = gpx[1] * w; dv[2] = gpx[2] * w;
+            dv[3] = tk * (G - S_after);
+            has = dv[0] != 0.f || dv[1] != 0.f || dv[2] != 0.f || dv[3] != 0.f;
+            if (has) cs.get(k, lane, nx, ny, nz);
+          }
+          warp_merged_scatter<float>(ra.g, grad, has, nx, ny, nz, dv, bk, lane);
+        } else if (bk != 0u) {
           const float w = al * tk;
           float dv[4] = {gpx[0] * w, gpx[1] * w, gpx[2] * w, tk * (G - S_after)};
           if (!(dv[0] != 0.f || dv[1] != 0.f || dv[2] != 0.f || dv[3] != 0.f)) continue;
@@ -406,12 +420,12 @@ inline unsigned grid_for(int64_t n, int threads = 256) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 1 << 20));
 }
 
-template <typename Store, int MODE, int K>
+template <typename Store, int MODE, int K, bool MERGE>
 int launch_batch_k(const BatchArgs& a, int threads, cudaStream_t s) {
   const int warps = threads / kWarp;
   const size_t tab = (((size_t)a.num_scenes * sizeof(pgb_scene)) + 15) & ~(size_t)15;
   const size_t smem = tab + (size_t)CoordStage<float, K>::kBytesPerWarp * warps;
-  auto kern = batch_train_kernel<Store, MODE, K>;
+  auto kern = batch_train_kernel<Store, MODE, K, MERGE>;
   int dev = 0;
   cudaGetDevice(&dev);
   static int configured[64] = {0};
@@ -432,15 +446,22 @@ int launch_batch_k(const BatchArgs& a, int threads, cudaStream_t s) {
   return after_launch();
 }
 
-template <typename Store, int MODE>
-int launch_batch_m(const BatchArgs& a, int K, int threads, cudaStream_t s) {
+template <typename Store, int MODE, bool MERGE>
+int launch_batch_km(const BatchArgs& a, int K, int threads, cudaStream_t s) {
   switch (K) {
-    case 1: return launch_batch_k<Store, MODE, 1>(a, threads, s);
-    case 2: return launch_batch_k<Store, MODE, 2>(a, threads, s);
-    case 4: return launch_batch_k<Store, MODE, 4>(a, threads, s);
-    case 8: return launch_batch_k<Store, MODE, 8>(a, threads, s);
+    case 1: return launch_batch_k<Store, MODE, 1, MERGE>(a, threads, s);
+    case 2: return launch_batch_k<Store, MODE, 2, MERGE>(a, threads, s);
+    case 4: return launch_batch_k<Store, MODE, 4, MERGE>(a, threads, s);
+    case 8: return launch_batch_k<Store, MODE, 8, MERGE>(a, threads, s);
     default: return PGB_ERR_ARG;
   }
+}
+
+template <typename Store, int MODE>
+int launch_batch_m(const BatchArgs& a, int K, int threads, int merge, cudaStream_t s) {
+  // nearest lookup scatters one cell per sample: no merged form
+  if (merge && MODE == PGB_TRILINEAR) return launch_batch_km<Store, MODE, true>(a, K, threads, s);
+  return launch_batch_km<Store, MODE, false>(a, K, threads, s);
 }
 
 }  // namespace
@@ -459,7 +480,7 @@ int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, 
                     const int32_t* ray_scene, int64_t num_rays, float term_threshold,
                     int32_t stratified, uint64_t seed, double loss_weight, float* rgba_out,
                     float* loss_out, void* workspace, int32_t slots_per_lane,
-                    int32_t threads_per_block, pgb_stream_t stream) {
+                    int32_t threads_per_block, int32_t merge_updates, pgb_stream_t stream) {
   if (!scenes || num_scenes <= 0 || num_scenes > kMaxScenes || num_rays < 0) return PGB_ERR_ARG;
   if (dtype != PGB_F32 && dtype != PGB_BF16) return PGB_ERR_UNSUPPORTED;
   if (mode != PGB_NEAREST && mode != PGB_TRILINEAR) return PGB_ERR_ARG;
@@ -489,11 +510,13 @@ int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, 
   a.work = reinterpret_cast<unsigned long long*>(workspace);
   a.ticket = reinterpret_cast<unsigned*>((char*)workspace + 8);
   a.ray_loss = reinterpret_cast<double*>((char*)workspace + 64);
+  const int merge = merge_updates ? 1 : 0;
   if (dtype == PGB_BF16)
-    return mode == PGB_NEAREST ? launch_batch_m<__nv_bfloat16, PGB_NEAREST>(a, K, threads, stream)
-                               : launch_batch_m<__nv_bfloat16, PGB_TRILINEAR>(a, K, threads, stream);
-  return mode == PGB_NEAREST ? launch_batch_m<float, PGB_NEAREST>(a, K, threads, stream)
-                             : launch_batch_m<float, PGB_TRILINEAR>(a, K, threads, stream);
+    return mode == PGB_NEAREST
+               ? launch_batch_m<__nv_bfloat16, PGB_NEAREST>(a, K, threads, merge, stream)
+               : launch_batch_m<__nv_bfloat16, PGB_TRILINEAR>(a, K, threads, merge, stream);
+  return mode == PGB_NEAREST ? launch_batch_m<float, PGB_NEAREST>(a, K, threads, merge, stream)
+                             : launch_batch_m<float, PGB_TRILINEAR>(a, K, threads, merge, stream);
 }
 
 int pgb_pack_mask(const uint8_t* mask, int64_t count, uint32_t* bits_out, pgb_stream_t stream) {

@@ -160,9 +160,10 @@ def test_invalid_scene_index_contributes_nothing():
     assert float(step.rgba[:10].abs().sum()) == 0.0
 
 
-@pytest.mark.parametrize("tiles", [(1, 256), (4, 128)])
+@pytest.mark.parametrize("tiles", [(1, 256), (4, 128), (1, 256, 1), (2, 256, 1)])
 def test_every_tile_gives_the_oracle_step(tiles):
-    """A 32-sample chunk per ray (K = 1) and a 128-sample one (K = 4) on the same batch."""
+    """A 32-sample chunk per ray (K = 1) and a 128-sample one (K = 4) on the same batch,
+    and the tiles whose scatter merges a warp's updates of the same cell."""
     problem = _make(torch.float32, seed=11)
     step, R = _batch(problem, term_threshold=0.0, tiles=tiles)
     loss = float(step.step())
@@ -190,7 +191,7 @@ def test_long_rays_take_a_tile_that_covers_them():
     step, R = _batch(problem, term_threshold=0.0)
     assert step.tiles[0] == 4
     times = step.autotune(reps=1)
-    assert all(32 * 32 * k >= S for k, _ in times)
+    assert all(32 * 32 * k >= S for k, *_ in times)
     loss = float(step.step())
     torch.cuda.synchronize()
     rgba_ref, grads, loss_ref = _oracle(problem, R)
