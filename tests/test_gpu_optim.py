@@ -81,33 +81,58 @@ def test_beta_loss_fused_in_the_train_kernel(mode):
 
 
 def test_training_steps_follow_the_reference_loop():
-    """Five steps of scripts/train.py:142-184 (nearest lookup, MSE + TV + beta, Adam)."""
+    """Five steps of scripts/train.py:142-184 (nearest lookup, MSE + TV + beta, Adam).
+
+    At every step the trainer's own gradient (render + beta + TV, as its Adam pass
+    receives it) is checked against the oracle's autograd gradient of the reference's loss
+    at the same pre-step grid, and the same gradient is fed to torch.optim.Adam, so that
+    differences cannot compound: after every step the grid, both moments and the |grad|
+    accumulator (:184) must agree with the reference optimiser to 1e-6 relative."""
     side, S, R = 24, 64, 400
     grid0 = torch.from_numpy(scenes.make_grid(side, 3, 71, amp=(0.2, 1.5)))
     T = torch.from_numpy(scenes.make_cameras(4, 72))
     imgs = torch.from_numpy(scenes.make_images(4, 8, 8, 73))
     pd, delta, lr, tv, beta = scenes.points_distance(side), 4.0 / S, 0.0075, 1e-5, 5e-3
     gmin = tp.grid_min(grid0.shape, pd)
-    ref = grid0.clone().requires_grad_(True)
-    topt = torch.optim.Adam([ref], lr=lr)
-    grid = grid0.to(DEV)
-    trainer = Trainer(grid, pd, S, delta, lr, tv=tv, beta=beta, mode="nearest")
+    ref = torch.nn.Parameter(grid0.clone())
+    topt = torch.optim.Adam([ref], lr=lr, foreach=False)
+    trainer = Trainer(grid0.to(DEV), pd, S, delta, lr, tv=tv, beta=beta, mode="nearest",
+                      fuse_tv=False)
+    captured = []
+    adam_step = trainer.opt.step
+
+    def spy(grad=None, zero_grad=True):
+        captured.append(grad.detach().clone())
+        return adam_step(grad, zero_grad)
+
+    trainer.opt.step = spy
+    acc = torch.zeros_like(grid0)
     for i in range(5):
         o, d, tgt = tp.camera_batch(T, 0.691, imgs, R, 80 + i, 2.0)
-        topt.zero_grad()
-        px, vals = tp.render_samples(ref, o, d, S, delta, gmin, pd, "nearest")
+        # the reference's loss and gradient at the trainer's pre-step grid
+        g = trainer.grid.detach().cpu().clone().requires_grad_(True)
+        px, vals = tp.render_samples(g, o, d, S, delta, gmin, pd, "nearest")
         mse = torch.nn.functional.mse_loss(px, tgt)
-        tvl = tv * tp.tv_loss(ref)
+        tvl = tv * tp.tv_loss(g)
         bl = beta * tp.beta_loss(vals[..., -1])
         (mse + tvl + bl).backward()
-        topt.step()
         losses = trainer.step_rays(o.to(DEV), d.to(DEV), tgt.to(DEV)).cpu()
-        np.testing.assert_allclose(losses.numpy(), [float(mse), float(tvl), float(bl)], rtol=1e-4)
-    # Adam turns tiny gradient differences into step-size differences on cells whose
-    # gradient is ~0; the grids agree to a few optimiser steps at most
-    diff = (trainer.grid.cpu() - ref.detach()).abs()
-    assert float(diff.max()) <= 5 * lr
-    assert float((diff > 1e-5).float().mean()) < 0.01
+        np.testing.assert_allclose(losses.numpy(), [float(mse), float(tvl), float(bl)], rtol=1e-5)
+        G = captured[-1].cpu()
+        scale = float(g.grad.abs().max())
+        assert float((G - g.grad).abs().max()) <= 1e-4 * scale, f"step {i}: gradient"
+        # the reference optimiser on the trainer's own gradient
+        ref.grad = G.clone()
+        topt.step()
+        acc += G.abs()
+        st = topt.state[ref]
+        for name, got, want in (("grid", trainer.grid, ref.detach()),
+                                ("exp_avg", trainer.opt.exp_avg, st["exp_avg"]),
+                                ("exp_avg_sq", trainer.opt.exp_avg_sq, st["exp_avg_sq"]),
+                                ("abs_grad", trainer.opt.abs_grad, acc)):
+            np.testing.assert_allclose(got.cpu().numpy(), want.numpy(), rtol=1e-6,
+                                       atol=1e-6 * float(want.abs().max()),
+                                       err_msg=f"step {i}: {name}")
 
 
 def test_fused_tv_adam_pass_equals_the_separate_passes():
