@@ -1,9 +1,10 @@
 """Benchmark of the fused render-path training step (forward + MSE + backward).
 
-Workload (dense 256^3 fp32 RGBA grid, 16 Gaussian blobs, box [-1.5,1.5]^3; 100 cameras of
-800x800 at radius 4 on the upper hemisphere, FOV 0.691 rad; 8192 random rays per step
-spread camera-major over the cameras, near 2, far 6, 256 stratified samples per ray,
-trilinear lookup). Synthetic seeded data stands in for the NeRF-synthetic scenes.
+Workload (dense 256^3 fp32 RGBA grid of 16 Gaussian blobs, box [-1.5,1.5]^3; 100 cameras of
+800x800 at radius 4 on the upper hemisphere, FOV 0.691 rad, whose target images are rendered
+from a second seeded ground-truth grid; 8192 random rays per step spread camera-major over
+the cameras, near 2, far 6, 256 stratified samples per ray, trilinear lookup). Synthetic
+seeded data stands in for the NeRF-synthetic scenes.
 
 A step = zero the dense gradient + one fused kernel that generates the rays from the
 resident cameras and images, samples, looks up, composites, takes the MSE gradient and
@@ -14,9 +15,9 @@ copied from pinned host memory every step and the loss copied back.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 `--impl reference` times the reference's algorithm on the host CPU (the oracle's
-restatement of it in PyTorch ops, all host threads) on a bounded sample of the same
-workload. Under torchrun with N > 1 each rank trains on its own ray batch with a
-replicated grid and the gradients are summed with one all-reduce per step.
+restatement of it in PyTorch ops, all host threads) on the same workload: every step is
+the full 8192-ray batch. Under torchrun with N > 1 each rank trains on its own ray batch
+with a replicated grid and the gradients are summed with one all-reduce per step.
 """
 from __future__ import annotations
 
@@ -38,12 +39,23 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import scenes  # noqa: E402  (seeded synthetic scene builder)
 
-WORKLOAD = dict(workload="train step, 256^3 fp32 grid, 100 cams 800x800, 8192 rays x 256 "
-                         "stratified samples, trilinear", grid=256, cameras=100, image=800,
-                rays=8192, samples=256, mode="trilinear", near=2.0, far=6.0, blobs=16,
-                camera_angle_x=0.691)
+WORKLOAD = dict(workload="train step, 256^3 fp32 grid, 100 cams 800x800 with targets rendered "
+                         "from a seeded ground-truth grid, 8192 rays x 256 stratified samples, "
+                         "trilinear", grid=256, cameras=100, image=800, rays=8192, samples=256,
+                mode="trilinear", near=2.0, far=6.0, blobs=16, rgb="sigmoid",
+                camera_angle_x=0.691, grid_seed=1, camera_seed=2, ground_truth_seed=4)
+# the precision form: 512^3 BF16 cells, 64 blobs, uniform RGB, 65536 rays from 200 cameras
+# of 800x800, 512 samples, compensated log-sum transmittance
+PRECISION = dict(workload="precision form, 512^3 grid (64 blobs, uniform RGB), 200 cams 800x800 "
+                          "with targets rendered from a seeded ground-truth grid, 65536 rays x 512 "
+                          "stratified samples, trilinear, log-sum transmittance", grid=512,
+                 cameras=200, image=800, rays=65536, samples=512, mode="trilinear", near=2.0,
+                 far=6.0, blobs=64, rgb="uniform", camera_angle_x=0.691, grid_seed=21,
+                 camera_seed=22, ground_truth_seed=23)
 NCU_TRAFFIC_BYTES = 446_778_112 + 35_163_904  # DRAM read + write, one launch
 METRIC = "train rays/sec (fwd+bwd)"
+# samples per chunk of the fused step (0: the library's choice)
+CHUNK = 0
 
 
 def _peaks():
@@ -55,13 +67,24 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def build_scene(dev, W):
-    side = W["grid"]
-    grid = torch.from_numpy(scenes.make_grid(side, W["blobs"], seed=1)).to(dev)
-    T = torch.from_numpy(scenes.make_cameras(W["cameras"], seed=2)).to(dev)
-    # targets: 100 x 800 x 800 RGBA fp32 = 1 GiB resident, seeded on the device
-    g = torch.Generator(device=dev).manual_seed(3)
-    imgs = torch.rand(W["cameras"], W["image"], W["image"], 4, device=dev, generator=g)
+def scene_grids(W):
+    """(trained grid, ground-truth grid) of a workload, float32 on the CPU, seeded."""
+    grid = scenes.make_grid_fast(W["grid"], W["blobs"], W["grid_seed"], rgb=W["rgb"])
+    gt = scenes.make_grid_fast(W["grid"], W["blobs"], W["ground_truth_seed"], rgb=W["rgb"])
+    return grid, gt
+
+
+def build_scene(pg, dev, W):
+    """The trained grid, the cameras and their target images ([C,H,W,4] fp32, resident:
+    1 GiB at 100 x 800^2), rendered on the GPU from the ground-truth grid along each
+    pixel's ray with the step's sampling."""
+    grid, gt = scene_grids(W)
+    grid = grid.to(dev)
+    T = torch.from_numpy(scenes.make_cameras(W["cameras"], seed=W["camera_seed"])).to(dev)
+    S = W["samples"]
+    imgs = pg.inference.render_camera_images(
+        gt.to(dev), T, W["image"], W["image"], W["camera_angle_x"], W["near"],
+        (W["far"] - W["near"]) / S, S, 3.0 / W["grid"], mode=W["mode"])
     return grid, T, imgs
 
 
@@ -117,53 +140,79 @@ class Clocks:
 
 
 def unique_cells(pg, grid, T, imgs, W, seed, delta, pd):
-    """U: distinct cells the step's in-bounds samples read (from the kernels' own index
-    math), the per-unit figure of the algorithmic byte count."""
-    idx, inb = pg.render.camera_sample_indices(
-        grid, T, imgs, W["camera_angle_x"], W["rays"], seed, W["near"], delta, W["samples"], pd,
-        mode=W["mode"], stratified=True, seed=7)
-    side = W["grid"]
+    """Per-unit figures of the algorithmic byte count, from the kernels' own index math on
+    one step's rays (trilinear): distinct cells read by in-bounds samples (all of them, as
+    the reference reads them), distinct cells of the live samples (in bounds with
+    transmittance > 0: the samples behind an opaque one have weight 0 and gradient 0 and
+    need not be read), and the in-bounds and live shares of the samples."""
+    S, side = W["samples"], W["grid"]
+    idx, inb, coords = pg.render.camera_sample_indices(
+        grid, T, imgs, W["camera_angle_x"], W["rays"], seed, W["near"], delta, S, pd,
+        mode="trilinear", stratified=True, seed=7, return_coords=True)
     lin = (idx[..., 0] * side + idx[..., 1]) * side + idx[..., 2]
-    lin = lin[inb] if W["mode"] == "nearest" else lin[inb.unsqueeze(-1).expand_as(lin)]
-    return int(torch.unique(lin).numel()), float(inb.float().mean())
+    all_cells = int(torch.unique(lin[inb.unsqueeze(-1).expand_as(lin)]).numel())
+    with torch.no_grad():
+        vals = pg.trilinear_interpolation(coords.reshape(-1, 3), idx.reshape(-1, 8, 3),
+                                          grid.float(), clip=True)
+    alpha = vals[:, 3].reshape(inb.shape) * inb
+    trans = torch.cumprod(torch.cat([torch.ones_like(alpha[:, :1]), 1 - alpha[:, :-1]], 1), 1)
+    live = inb & (trans > 0)
+    live_cells = int(torch.unique(lin[live.unsqueeze(-1).expand_as(lin)]).numel())
+    shares = float(inb.float().mean()), float(live.float().mean())
+    del idx, lin, coords, vals
+    return live_cells, all_cells, shares[0], shares[1]
 
 
-def cpu_reference_rate(W, grid_cpu, T_cpu, imgs_cpu, budget_s=12.0, rays=1024):
-    """The reference's path on the host cores: oracle port, fp32 autograd, all threads.
-    Bounded sample: `rays` rays per step of the same scene and sampling, repeated until
-    budget_s of work (at least 2 timed steps after one warm-up)."""
+def reference_cpu_steps(W, steps, warmup, budget_s=None):
+    """The reference's training step on the host cores: the oracle's restatement of
+    scripts/train.py:142-156, 181 in torch CPU ops (fp32 autograd, all host threads) on the
+    full workload: every step is one fwd+bwd of W["rays"] camera rays (counter-hash pixel
+    positions, as the GPU arm draws them) x W["samples"] stratified samples on the seeded
+    grid, with targets rendered by the oracle from the ground-truth grid along the same
+    rays (untimed). `warmup` untimed steps, then `steps` timed ones (fewer when budget_s of
+    timed work runs out first, at least 2). Returns (median seconds per timed step, timed
+    steps, threads)."""
     from oracle import torch_port as tp
     torch.set_num_threads(os.cpu_count() or 1)
+    grid, gt = scene_grids(W)
+    T = torch.from_numpy(scenes.make_cameras(W["cameras"], seed=W["camera_seed"]))
     pd = 3.0 / W["grid"]
-    S = W["samples"]
+    S, R = W["samples"], W["rays"]
     delta = (W["far"] - W["near"]) / S
-    gmin = tp.grid_min(grid_cpu.shape, pd)
-
-    def one(step):
-        o, d, target = tp.camera_batch(T_cpu, W["camera_angle_x"], imgs_cpu, rays, 1000 + step,
-                                       W["near"])
-        jit = tp.jitter_for(7, rays, S)
-        g = grid_cpu.detach().requires_grad_(True)
+    gmin = tp.grid_min(grid.shape, pd)
+    jit = tp.jitter_for(7, R, S)
+    frame = torch.zeros(1, W["image"], W["image"], 4).expand(W["cameras"], -1, -1, -1)
+    times = []
+    for i in range(warmup + steps):
+        o, d, _ = tp.camera_batch(T, W["camera_angle_x"], frame, R, 1000 + i, W["near"])
+        with torch.no_grad():
+            target = tp.render(gt, o, d, S, delta, gmin, pd, W["mode"], True, jit)
+        g = grid.detach().requires_grad_(True)
         t0 = time.perf_counter()
         loss = tp.train_loss(g, o, d, target, S, delta, gmin, pd, W["mode"], True, jit)
         loss.backward()
-        return time.perf_counter() - t0
-
-    one(0)
-    times = []
-    start = time.perf_counter()
-    while len(times) < 2 or (time.perf_counter() - start < budget_s and len(times) < 20):
-        times.append(one(len(times) + 1))
-    med = statistics.median(times)
-    return dict(value=rays / med, unit="rays/s", cores=torch.get_num_threads(), kind="port",
-                sample=f"{rays} rays/step of the same workload (256^3 grid, 256 stratified samples, "
-                       f"trilinear), fwd+bwd, median of {len(times)} steps after 1 warm-up; "
-                       "oracle restatement in torch CPU ops, fp32")
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+            if budget_s is not None and len(times) >= 2 and sum(times) >= budget_s:
+                break
+    return statistics.median(times), len(times), torch.get_num_threads()
 
 
-def torch_gpu_rate(W, grid, T, imgs, dev, steps=3):
+def cpu_reference_rate(W, budget_s=15.0):
+    """cpu_baseline: the reference's step on the host cores (reference_cpu_steps), one
+    warm-up step and up to 20 timed ones within budget_s."""
+    sec, n, threads = reference_cpu_steps(W, 20, 1, budget_s)
+    return dict(value=W["rays"] / sec, unit="rays/s", cores=threads, kind="port",
+                sample=f"the full workload ({W['rays']} rays x {W['samples']} stratified samples, "
+                       f"{W['grid']}^3, {W['mode']}) per step, fwd+bwd, median of {n} steps after "
+                       "1 warm-up; oracle restatement in torch CPU ops, fp32, all host threads")
+
+
+def torch_gpu_rate(W, grid, T, imgs, dev, steps=10, warmup=2):
     """The reference's algorithm as plain torch ops on the same GPU (oracle port with
-    CUDA tensors; CUDA-event timed)."""
+    CUDA tensors): `warmup` untimed steps, then `steps` steps timed with CUDA events, the
+    SM clocks sampled around them."""
     from oracle import torch_port as tp
     pd = 3.0 / W["grid"]
     S = W["samples"]
@@ -179,17 +228,20 @@ def torch_gpu_rate(W, grid, T, imgs, dev, steps=3):
         loss = tp.train_loss(g, o, d, target, S, delta, gmin, pd, W["mode"], True, jit)
         loss.backward()
 
-    one()
+    for _ in range(warmup):
+        one()
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(steps):
-        one()
-    e1.record()
-    torch.cuda.synchronize(dev)
+    with Clocks(dev.index) as clk:
+        e0.record()
+        for _ in range(steps):
+            one()
+        e1.record()
+        torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1) / steps
     return dict(value=R / (ms / 1e3), unit="rays/s", ms_per_step=ms, kind="port",
-                sample=f"{R} rays x {S} samples, same scene, {steps} steps after 1 warm-up")
+                clocks=clk.summary(),
+                sample=f"{R} rays x {S} samples, same scene, {steps} steps after {warmup} warm-up")
 
 
 def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup, mode=None):
@@ -198,7 +250,8 @@ def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup, mode=None):
     S, R = W["samples"], W["rays"]
     g = grid.to(dtype)
     step = pg.FusedTrainStep(g, 3.0 / W["grid"], S, (W["far"] - W["near"]) / S,
-                             mode=mode or W["mode"], stratified=True, seed=7, overlap_zero=True)
+                             mode=mode or W["mode"], stratified=True, seed=7, overlap_zero=True,
+                             chunk_samples=CHUNK)
     stream = torch.cuda.current_stream(dev)
     for i in range(warmup):
         step.step_cameras(T, imgs, W["camera_angle_x"], R, 5000 + i, near=W["near"])
@@ -264,8 +317,9 @@ def random_access_ceiling(pg, dev, reads=1 << 24, reps=5):
     """The GPU's rate for independent random 32 B sectors out of a 256 MiB buffer (16 B
     loads, and float4 atomic adds), each launch after a 256 MiB write that evicts L2:
     the ceiling for gathers and scatters with no reuse, as the render kernels do."""
-    from plenoxels_gb300 import _lib
+    from plenoxels_gb300 import _lib, probes
     lib = _lib.load()
+    plib = probes.load()
     stream = torch.cuda.current_stream(dev).cuda_stream
     nbytes = 256 << 20
     table = torch.zeros(nbytes // 4, device=dev)
@@ -280,9 +334,9 @@ def random_access_ceiling(pg, dev, reads=1 << 24, reps=5):
             _lib.check(lib.pgb_fill_zero(flush.data_ptr(), nbytes, stream), "pgb_fill_zero")
             e0.record()
             if kind == "reads":
-                st = lib.pgb_probe_random_reads(table.data_ptr(), nbytes, n, 17 + rep, sink.data_ptr(), stream)
+                st = plib.pgb_probe_random_reads(table.data_ptr(), nbytes, n, 17 + rep, sink.data_ptr(), stream)
             else:
-                st = lib.pgb_probe_random_atomics(table.data_ptr(), nbytes, n, 17 + rep, stream)
+                st = plib.pgb_probe_random_atomics(table.data_ptr(), nbytes, n, 17 + rep, stream)
             e1.record()
             _lib.check(st, "pgb_probe_random_" + kind)
             torch.cuda.synchronize(dev)
@@ -353,8 +407,9 @@ def batched_leg(pg, dev, steps=30, seed=11, num_scenes=64):
     occ_cells = sum(int(sc.occupancy.sum()) for sc in scs)
     return {"value": R / (statistics.median(ms) / 1e3), "unit": "rays/s", "rays_per_step": R,
             "scenes": len(scs), "cells": cells, "occupied_cells": occ_cells, "samples": S,
-            "p50_ms": p50, "p99_ms": p99, "tiles": {f"K{k}_t{t}": v for (k, t), v in tiles.items()},
-            "chosen_tile": f"K{step.tiles[0]}_t{step.tiles[1]}",
+            "p50_ms": p50, "p99_ms": p99,
+            "tiles": {f"K{k}_t{t}" + ("_merge" if m else ""): v for (k, t, m), v in tiles.items()},
+            "chosen_tile": f"K{step.tiles[0]}_t{step.tiles[1]}" + ("_merge" if step.tiles[2] else ""),
             "chosen_brick_cells": 1 << step.brick_log2,
             "note": "BF16 cells, occupancy-masked fp32 gradients, early termination at T<1e-4, "
                     "CUDA-graph replay of zeroing + one persistent launch; same rays every step"}
@@ -408,50 +463,66 @@ def full_step_leg(pg, grid, T, imgs, W, dev, steps, warmup):
                     "|grad| accumulation; dense fp32 grid of 256^3"}
 
 
-def run_reference_arm(args, W, rays=512):
-    """--impl reference: the reference's algorithm on the host cores (the oracle's torch
-    restatement, fp32 autograd, all threads). Each step is one fwd+bwd over a bounded
-    sample of `rays` rays of the same workload; W untimed steps, then K timed ones."""
+def run_reference_arm(args, W):
+    """--impl reference: the reference's training step on the host cores (the oracle's
+    torch restatement, fp32 autograd, all threads), each step the full workload of
+    W["rays"] rays; W untimed steps, then K timed ones."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from oracle import torch_port as tp
-    torch.set_num_threads(os.cpu_count() or 1)
-    grid = torch.from_numpy(scenes.make_grid(W["grid"], W["blobs"], seed=1))
-    T = torch.from_numpy(scenes.make_cameras(W["cameras"], seed=2))
-    g = torch.Generator().manual_seed(3)
-    imgs = torch.rand(W["cameras"], W["image"], W["image"], 4, generator=g)
-    pd = 3.0 / W["grid"]
-    S = W["samples"]
-    delta = (W["far"] - W["near"]) / S
-    gmin = tp.grid_min(grid.shape, pd)
-    jit = tp.jitter_for(7, rays, S)
-    times = []
-    for i in range(args.warmup + args.steps):
-        o, d, target = tp.camera_batch(T, W["camera_angle_x"], imgs, rays, 1000 + i, W["near"])
-        gg = grid.detach().requires_grad_(True)
-        t0 = time.perf_counter()
-        loss = tp.train_loss(gg, o, d, target, S, delta, gmin, pd, W["mode"], True, jit)
-        loss.backward()
-        dt = time.perf_counter() - t0
-        if i >= args.warmup:
-            times.append(dt)
-    value = rays / statistics.median(times)
-    cores = torch.get_num_threads()
-    sample = (f"{rays} rays/step of the same workload (256^3 grid, 256 stratified samples, "
-              f"trilinear), fwd+bwd, median of {len(times)} steps after {args.warmup} warm-up; "
-              "oracle restatement in torch CPU ops, fp32")
+    sec, n, cores = reference_cpu_steps(W, args.steps, args.warmup)
+    value = W["rays"] / sec
+    sample = (f"the full workload ({W['rays']} rays x {W['samples']} stratified samples, "
+              f"{W['grid']}^3, {W['mode']}) per step, fwd+bwd, median of {n} steps after "
+              f"{args.warmup} warm-up; oracle restatement in torch CPU ops, fp32, all host threads")
     line = {"metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * W["rays"] / value,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "impl": "reference",
-            "config": dict(W, step=f"per step a bounded sample of {rays} rays; ms_per_step scaled "
-                                   f"to {W['rays']} rays"),
+            "data": "synthetic", "impl": "reference", "config": dict(W),
             "cpu_baseline": {"value": value, "unit": "rays/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def precision_leg(pg, dev, steps, warmup):
+    """The precision form: a 512^3 grid of 64 blobs with BF16 cells, 65536 rays per step
+    from 200 cameras of 800x800, 512 stratified samples, compensated log-sum
+    transmittance; the same step with fp32 cells beside it, and both with the product
+    transmittance. Rays/s of the whole step (gradient zeroing + fused launch) and the
+    fused kernel's time, for each form."""
+    P = PRECISION
+    grid, T, imgs = build_scene(pg, dev, P)
+    S, R = P["samples"], P["rays"]
+    out = {"workload": P["workload"]}
+    forms = [("bf16_logsum", torch.bfloat16, "logsum"), ("f32_logsum", torch.float32, "logsum"),
+             ("bf16_product", torch.bfloat16, "product"), ("f32_product", torch.float32, "product")]
+    stream = torch.cuda.current_stream(dev)
+    for name, dt, trans in forms:
+        g = grid.to(dt)
+        st = pg.FusedTrainStep(g, 3.0 / P["grid"], S, (P["far"] - P["near"]) / S, mode=P["mode"],
+                               stratified=True, seed=7, overlap_zero=True, transmittance=trans,
+                               chunk_samples=CHUNK)
+        for i in range(warmup):
+            st.step_cameras(T, imgs, P["camera_angle_x"], R, 5000 + i, near=P["near"])
+        torch.cuda.synchronize(dev)
+        st.kernel_events = []
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for i in range(steps):
+            st.step_cameras(T, imgs, P["camera_angle_x"], R, 6000 + i, near=P["near"])
+        t1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = t0.elapsed_time(t1) / steps
+        kern = sum(a.elapsed_time(b) for a, b in st.kernel_events) / steps
+        out[name] = {"value": R / (ms / 1e3), "unit": "rays/s", "ms_per_step": ms, "kernel_ms": kern}
+        del st, g
+    out["bf16_over_f32_logsum"] = out["bf16_logsum"]["value"] / out["f32_logsum"]["value"]
+    out["bf16_over_f32_product"] = out["bf16_product"]["value"] / out["f32_product"]["value"]
+    del grid, imgs
+    torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -462,6 +533,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-baselines", action="store_true", help="skip the CPU and torch-GPU legs")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched multi-scene leg")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 512^3 precision-form leg")
     ap.add_argument("--batched-only", action="store_true", help="run only the batched leg")
     ap.add_argument("--batched-scenes", type=int, default=64, help="scenes of the batched leg")
     args = ap.parse_args()
@@ -492,11 +564,11 @@ def main():
     S, R = W["samples"], W["rays"]
     pd = 3.0 / W["grid"]
     delta = (W["far"] - W["near"]) / S
-    grid, T, imgs = build_scene(dev, W)
+    grid, T, imgs = build_scene(pg, dev, W)
     from plenoxels_gb300.distributed import allreduce_gradient
     # weak scaling: R rays per rank, each rank's MSE weighted by its share of R * world
     step = pg.FusedTrainStep(grid, pd, S, delta, mode=W["mode"], stratified=True, seed=7,
-                             loss_weight=1.0 / world, overlap_zero=True)
+                             loss_weight=1.0 / world, overlap_zero=True, chunk_samples=CHUNK)
     stream = torch.cuda.current_stream(dev)
 
     def train(i):
@@ -615,11 +687,13 @@ def main():
             torch.distributed.destroy_process_group()
         return
 
-    # roofline of the fused kernel: algorithmic bytes per launch / measured duration.
+    # roofline of the fused kernel: algorithmic bytes per launch / its measured duration.
     # traffic: dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on
-    # this workload under ncu (profiles/render_train_trilinear_256cube_ncu.md)
-    U, inb_frac = unique_cells(pg, grid, T, imgs, W, 1000 * rank + args.warmup, delta, pd)
+    # this workload under ncu
+    U, U_all, inb_frac, live_frac = unique_cells(pg, grid, T, imgs, W, 1000 * rank + args.warmup,
+                                                 delta, pd)
     alg_bytes = U * 16 + U * 16 + R * 60
+    alg_all = U_all * 16 + U_all * 16 + R * 60
     peak, peak_kind = _peaks()
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -627,6 +701,12 @@ def main():
                 "traffic_unit": "bytes per launch (ncu capture of this workload)",
                 "kernel": "render_kernel<trilinear,train>",
                 "kernel_ms": kern_ms, "unique_cells": U, "algorithmic_bytes": alg_bytes,
+                "unique_cells_definition": "distinct cells of the live samples (in bounds, "
+                                           "transmittance > 0); samples behind an opaque one "
+                                           "need not be read",
+                "unique_cells_all_samples": U_all, "algorithmic_bytes_all_samples": alg_all,
+                "frac_all_samples": alg_all / (kern_ms / 1e3) / 1e9 / peak,
+                "in_bounds_sample_share": inb_frac, "live_sample_share": live_frac,
                 "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "issued_gather_bytes": int(R * S * inb_frac * 8 * 16),
                 "step_bytes": alg_bytes + grid.numel() * 4}
@@ -636,6 +716,7 @@ def main():
             "data": "synthetic",
             "config": dict(W, l2="inputs larger than L2: 256 MiB grid read and 256 MiB gradient "
                                  "zeroed + scattered every step, 1 GiB of target images",
+                           chunk_samples=CHUNK,
                            parallelism=f"dp{world}" if world > 1 else "single"),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "clocks": clk.summary()}
@@ -656,13 +737,16 @@ def main():
     line["nearest_lookup"] = nearest
     line["drop_in_path"] = drop_in_leg(pg, grid, T, imgs, W, dev, args.steps, args.warmup)
     line["full_training_step"] = full_step_leg(pg, grid, T, imgs, W, dev, args.steps, args.warmup)
+    if not args.no_baselines:
+        line["torch_gpu_baseline"] = torch_gpu_rate(W, grid, T, imgs, dev)
+    del step, grid, imgs
+    torch.cuda.empty_cache()
+    if not args.no_precision:
+        line["precision_form"] = precision_leg(pg, dev, args.steps, args.warmup)
     if not args.no_batched:
-        del step
         line["batched_form"] = batched_leg(pg, dev)
     if not args.no_baselines:
-        grid_cpu, T_cpu, imgs_cpu = grid.cpu(), T.cpu(), imgs.cpu()
-        line["torch_gpu_baseline"] = torch_gpu_rate(W, grid, T, imgs, dev)
-        line["cpu_baseline"] = cpu_reference_rate(W, grid_cpu, T_cpu, imgs_cpu)
+        line["cpu_baseline"] = cpu_reference_rate(W)
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

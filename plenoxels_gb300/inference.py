@@ -76,3 +76,36 @@ def visulize_3d_in_2d(grid_cells_data, transform_matrices, camera_angle_x, imgs,
     image = torch.empty(side, side, 4, dtype=torch.uint8, device=grid.device)
     check(lib.pgb_rgba_to_image(ptr(rgba), side, ptr(image), s), "visulize_3d_in_2d")
     return image.cpu().numpy()
+
+
+@torch.no_grad()
+def render_camera_images(grid, transforms, height, width, camera_angle_x, near, delta_step,
+                         num_samples, points_distance, mode="trilinear", grid_min=None,
+                         stratified=False, seed=0):
+    """Premultiplied RGBA images [C, height, width, 4] (float32, on the grid's device) of
+    a grid seen from each camera: pixel (row, col) is the composited ray of the uniforms
+    u = col / height, v = row / width, the ray that generate_rays_batched
+    (src/ray_sampling.py:195-264) maps back to that pixel, started `near` along its
+    direction and sampled as the training step samples. One fused forward launch per
+    camera. Square images only, as the reference indexes them. No counterpart in the
+    reference beyond the per-ray forward it composes (it trains against photographs)."""
+    require_cuda(grid, transforms)
+    if height != width:
+        raise ValueError("render_camera_images renders square images")
+    from .render import render_rays
+    dev = grid.device
+    C, H, W = transforms.shape[0], int(height), int(width)
+    rows = torch.arange(H, device=dev, dtype=torch.float32)
+    cols = torch.arange(W, device=dev, dtype=torch.float32)
+    uv = torch.stack([(cols / H).expand(H, W), (rows / W)[:, None].expand(H, W)], -1).reshape(1, H * W, 2)
+    blank = torch.zeros(1, H, W, 4, device=dev)
+    out = torch.empty(C, H, W, 4, dtype=torch.float32, device=dev)
+    g = grid.detach().contiguous()
+    for c in range(C):
+        T = transforms[c:c + 1].contiguous()
+        dirs, _ = generate_rays_batched(blank, H * W, T, camera_angle_x, device=dev, ray_uv=uv)
+        origins = (T[0, :3, 3] + near * dirs).contiguous()
+        rgba = render_rays(g, origins, dirs, delta_step, num_samples, points_distance, grid_min,
+                           mode=mode, stratified=stratified, seed=seed)
+        out[c] = rgba.reshape(H, W, 4)
+    return out
