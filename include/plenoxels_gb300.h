@@ -89,6 +89,10 @@ typedef struct {
                                masked by the clamp, or a second opaque sample was read):
                                results are unchanged and the rest of the ray is never read.
                                Tuning only. */
+  int64_t first_ray;        /* index of this batch's first ray in the stratification stream
+                               (0 for a batch of its own): ranks that split one batch of
+                               explicit rays pass their share's offset, and every ray is
+                               sampled as in the unsplit batch */
 } pgb_rays;
 
 /* ---- fused render path (scripts/train.py:142-156 composed with src/ray_sampling.py,

@@ -64,6 +64,7 @@ class PgbRays(Structure):
         ("background", c_float * 3),
         ("log_transmittance", c_int32),
         ("chunk_samples", c_int32),
+        ("first_ray", c_int64),
     ]
 
 

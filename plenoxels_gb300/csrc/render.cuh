@@ -59,6 +59,7 @@ struct RenderArgs {
   Real delta;
   int stratified;
   uint64_t strat_seed;
+  int64_t first_ray;  // index of ray 0 in the stratification stream
   float term_thr;
   int chunk_samples;  // host-side chunk request (pick_slots)
   int use_bg;      // rgb += (1 - A) * bg after compositing
@@ -156,7 +157,7 @@ __device__ __forceinline__ void load_ray(const RenderArgs<Real>& a, int64_t r, R
       for (int c = 0; c < 4; ++c) ray.tgt[c] = a.target[4 * r + c];
     }
   }
-  ray.h = a.stratified ? hash_stream(a.strat_seed, (uint64_t)r) : 0ull;
+  ray.h = a.stratified ? hash_stream(a.strat_seed, (uint64_t)(r + a.first_ray)) : 0ull;
 }
 
 // Normalised grid coordinates of sample s (0-based) of a ray:

@@ -36,7 +36,7 @@ def _transmittance(name: str) -> int:
 
 
 def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, seed, term_threshold,
-               cameras=None, background=None, log_t=0, chunk_samples=0) -> PgbRays:
+               cameras=None, background=None, log_t=0, chunk_samples=0, first_ray=0) -> PgbRays:
     r = PgbRays()
     r.origins = ptr(origins)
     r.dirs = ptr(dirs)
@@ -52,6 +52,7 @@ def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, see
         r.background[:] = [float(v) for v in background]
     r.log_transmittance = int(log_t)
     r.chunk_samples = int(chunk_samples)
+    r.first_ray = int(first_ray)
     return r
 
 
@@ -314,15 +315,17 @@ class FusedTrainStep:
             self.kernel_events.append(ev)
         return self.loss
 
-    def step_rays(self, origins, dirs, target, rgba_out=None, zero_grad=True):
-        """Explicit rays [R,3] and their target pixels [R,4]."""
+    def step_rays(self, origins, dirs, target, rgba_out=None, zero_grad=True, first_ray=0):
+        """Explicit rays [R,3] and their target pixels [R,4]. first_ray: index of the first
+        of these rays in the stratification stream, for ranks that each take a share of
+        one batch (distributed.shard_rays) and must sample it as the whole batch would."""
         require_cuda(origins, dirs, target)
         _check_rays(self.grid, origins, dirs)
         if target.shape != (origins.shape[0], 4) or target.dtype != self.real:
             raise ValueError(f"target must be [R,4] {self.real}")
         rdesc = _rays_desc(origins, dirs, origins.shape[0], self.num_samples, self.delta_step,
                            self.stratified, self.seed, self.term_threshold, background=self.background,
-                           log_t=self.log_t, chunk_samples=self.chunk_samples)
+                           log_t=self.log_t, chunk_samples=self.chunk_samples, first_ray=first_ray)
         return self._launch(rdesc, target.contiguous(), rgba_out, zero_grad)
 
     def step_cameras(self, transforms, images, camera_angle_x, num_rays, ray_seed, near=0.0,

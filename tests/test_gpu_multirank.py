@@ -2,7 +2,8 @@
 
 Two processes share the one GPU. Each runs the product FusedTrainStep on its contiguous
 share of the rays with its MSE weighted by its share of the global ray count
-(distributed.shard_rays / loss_weight). Their gradients and losses are summed over a
+(distributed.shard_rays / loss_weight) and its offset in the batch's stratification
+stream (first_ray). Their gradients and losses are summed over a
 gloo group on CPU copies, and the sums must equal one process running the same step on
 all rays (scripts/train.py:156 takes the mean over all rays). No kernel waits on another
 process: the only exchange is the host-side sum after each process's step has finished.
@@ -40,11 +41,11 @@ def _scene():
     return grid, o, d, tgt, side, S
 
 
-def _step(grid, o, d, tgt, side, S, weight, mode):
+def _step(grid, o, d, tgt, side, S, weight, mode, first_ray=0):
     import plenoxels_gb300 as pg
     st = pg.FusedTrainStep(grid.cuda(), 3.0 / side, S, 4.0 / S, mode=mode, stratified=True,
                            seed=5, loss_weight=weight)
-    loss = st.step_rays(o.cuda(), d.cuda(), tgt.cuda())
+    loss = st.step_rays(o.cuda(), d.cuda(), tgt.cuda(), first_ray=first_ray)
     torch.cuda.synchronize()
     return float(loss), st.grad.cpu()
 
@@ -60,7 +61,8 @@ def _rank_main(rank, world, port, out, mode):
     grid, o, d, tgt, side, S = _scene()
     start, count = shard_rays(o.shape[0], rank, world)
     sl = slice(start, start + count)
-    loss, grad = _step(grid, o[sl], d[sl], tgt[sl], side, S, loss_weight(count, o.shape[0]), mode)
+    loss, grad = _step(grid, o[sl], d[sl], tgt[sl], side, S, loss_weight(count, o.shape[0]), mode,
+                       first_ray=start)
     allreduce_gradient(grad)
     lsum = torch.tensor([loss], dtype=torch.float64)
     dist.all_reduce(lsum)
