@@ -781,10 +781,22 @@ render_kernel(const RenderArgs<Real> a) {
       last_block = __shfl_sync(kFull, last_block, 0);
       if (last_block) {
         __threadfence();
+        // block partials in block order, eight loads in flight per lane (L2 reads: the
+        // partials were written by other blocks before their ticket)
         double sum = 0.0, bsum = 0.0;
-        for (unsigned i = lane; i < gridDim.x; i += kWarp) {
-          sum += *((volatile double*)a.partials + i);
-          if (with_beta) bsum += *((volatile double*)a.partials_beta + i);
+        for (unsigned i0 = lane; i0 < gridDim.x; i0 += 8 * kWarp) {
+          double p[8], q[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const unsigned i = i0 + u * kWarp;
+            p[u] = i < gridDim.x ? __ldcg(a.partials + i) : 0.0;
+            q[u] = (with_beta && i < gridDim.x) ? __ldcg(a.partials_beta + i) : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            sum += p[u];
+            bsum += q[u];
+          }
         }
         sum = warp_sum(sum);
         bsum = warp_sum(bsum);
