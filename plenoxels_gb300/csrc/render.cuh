@@ -19,8 +19,9 @@
 //     S_s = G_s * alpha_s + (1 - alpha_s) * S_{s+1},  S_{end} = 0,
 // a suffix recurrence of affine maps evaluated with a second warp scan. It contains no
 // division, so alpha == 1 (transmittance exactly 0 after the clip) is exact. Per-sample
-// values stay in registers; with more than one chunk the earlier chunks are re-gathered
-// in the reverse pass (the transmittance at each chunk start is kept in lane c).
+// values of the current chunk stay in registers; in the reverse pass the chunks before the
+// last come back from the warp's shared-memory stage (the last few chunks) or are gathered
+// again from the grid (the transmittance at each chunk start is kept in lane c).
 #pragma once
 
 #include "pgb_device.cuh"
@@ -425,6 +426,61 @@ struct CoordStage {
   }
 };
 
+// Chunks of 32 samples whose values the render kernel keeps per warp for its reverse pass.
+#ifndef PGB_STAGE_CHUNKS
+#define PGB_STAGE_CHUNKS 4
+#endif
+
+// The render kernel's per-warp shared-memory stage. It holds the normalised coordinates of
+// the last M chunks, so the reverse pass does not recompute the stratification hash and
+// the exact divisions. With 32-sample chunks (K = 1, M = PGB_STAGE_CHUNKS) it also holds
+// their clamped values and clamp-pass bits, so the reverse pass reads the M - 1 chunks
+// before the last from here instead of gathering them from the grid again. Layout
+// [slot][field][K][32]: each lane reads back only what it wrote, without bank conflicts.
+template <typename Real, int K>
+struct ChunkStage {
+  static constexpr int M = K == 1 ? PGB_STAGE_CHUNKS : 1;
+  static_assert((M & (M - 1)) == 0, "stage slots must be a power of two");
+  static constexpr int kCoordBytes = 3 * K * kWarp * (int)sizeof(Real);
+  static constexpr int kValBytes = M > 1 ? 4 * K * kWarp * (int)sizeof(Real) + K * kWarp * 4 : 0;
+  static constexpr int kSlotBytes = kCoordBytes + kValBytes;
+  static constexpr int kBytesPerWarp = M * kSlotBytes;
+  unsigned char* base;
+  __device__ __forceinline__ ChunkStage(unsigned char* all, int warp)
+      : base(all + (size_t)warp * kBytesPerWarp) {}
+  __device__ __forceinline__ unsigned char* slot(int c) const { return base + (c & (M - 1)) * kSlotBytes; }
+  // chunk c is still in the stage when the reverse pass reaches it (last = last chunk)
+  __device__ __forceinline__ static bool holds(int c, int last) { return M > 1 && c > last - M; }
+  __device__ __forceinline__ void put(int c, int k, int lane, Real x, Real y, Real z) {
+    Real* n = reinterpret_cast<Real*>(slot(c));
+    n[(0 * K + k) * kWarp + lane] = x;
+    n[(1 * K + k) * kWarp + lane] = y;
+    n[(2 * K + k) * kWarp + lane] = z;
+  }
+  __device__ __forceinline__ void get(int c, int k, int lane, Real& x, Real& y, Real& z) const {
+    const Real* n = reinterpret_cast<const Real*>(slot(c));
+    x = n[(0 * K + k) * kWarp + lane];
+    y = n[(1 * K + k) * kWarp + lane];
+    z = n[(2 * K + k) * kWarp + lane];
+  }
+  __device__ __forceinline__ void put_vals(int c, int k, int lane, const Real v[4], uint32_t bits) {
+    if constexpr (M > 1) {
+      Real* w = reinterpret_cast<Real*>(slot(c) + kCoordBytes);
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) w[(ch * K + k) * kWarp + lane] = v[ch];
+      reinterpret_cast<uint32_t*>(slot(c) + kCoordBytes + 4 * K * kWarp * sizeof(Real))[k * kWarp + lane] = bits;
+    }
+  }
+  __device__ __forceinline__ void get_vals(int c, int k, int lane, Real v[4], uint32_t& bits) const {
+    if constexpr (M > 1) {
+      const Real* w = reinterpret_cast<const Real*>(slot(c) + kCoordBytes);
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) v[ch] = w[(ch * K + k) * kWarp + lane];
+      bits = reinterpret_cast<const uint32_t*>(slot(c) + kCoordBytes + 4 * K * kWarp * sizeof(Real))[k * kWarp + lane];
+    }
+  }
+};
+
 #ifndef PGB_RENDER_GATHER_INLINE
 #define PGB_RENDER_GATHER_INLINE 1
 #endif
@@ -447,7 +503,7 @@ PGB_RENDER_GATHER_ATTR void render_sample(const RenderArgs<Real>& a, const Ray<R
 template <typename Real, typename Store, int MODE, int K, bool ADJ>
 __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ray<Real>& ray, int c,
                                              int lane, Real v[K][4], uint32_t bits[K],
-                                             CoordStage<Real, K>& cs) {
+                                             ChunkStage<Real, K>& cs) {
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     const int s = (c * K + k) * kWarp + lane;
@@ -456,7 +512,7 @@ __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ra
     if (s < a.S) {
       Real nx, ny, nz;
       render_sample<Real, Store, MODE>(a, ray, s, v[k], bits[k], nx, ny, nz);
-      if (ADJ && PGB_COORDS_IN_SMEM) cs.put(k, lane, nx, ny, nz);
+      if (ADJ) cs.put(c, k, lane, nx, ny, nz);
     }
   }
 }
@@ -544,7 +600,7 @@ __device__ __forceinline__ Real pick4(const Real v[4], int i) {
 
 template <typename Real, int K>
 constexpr int render_smem_bytes(int warps_per_block) {
-  return CoordStage<Real, K>::kBytesPerWarp * warps_per_block;
+  return ChunkStage<Real, K>::kBytesPerWarp * warps_per_block;
 }
 
 template <int MODE, int K>
@@ -566,7 +622,7 @@ render_kernel(const RenderArgs<Real> a) {
   const int64_t gw = (int64_t)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int64_t nw = (int64_t)gridDim.x * warps_per_block;
   const int nchunks = (a.S + kWarp * K - 1) / (kWarp * K);
-  CoordStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
+  ChunkStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
   double loss_lane = 0.0;
   double beta_lane = 0.0;
   const bool with_beta = PHASE == kTrain && a.beta_w != 0.0;
@@ -612,6 +668,10 @@ render_kernel(const RenderArgs<Real> a) {
       }
       __syncwarp();
       gather_chunk<Real, Store, MODE, K, ADJ>(a, ray, c, lane, v, bits, cs);
+      if (ADJ) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) cs.put_vals(c, k, lane, v[k], bits[k]);
+      }
       if constexpr (LOGT) {
         scan_chunk_log<K>(v, LT, LC, lane, Ts);
         T = isinf(LT) ? Real(0) : (Real)expf(LT + LC);
@@ -689,7 +749,12 @@ render_kernel(const RenderArgs<Real> a) {
     for (int c = last; c >= 0; --c) {
       if (c != last) {
         __syncwarp();
-        gather_chunk<Real, Store, MODE, K, true>(a, ray, c, lane, v, bits, cs);
+        if (ChunkStage<Real, K>::holds(c, last)) {  // the chunk's values are still staged
+#pragma unroll
+          for (int k = 0; k < K; ++k) cs.get_vals(c, k, lane, v[k], bits[k]);
+        } else {
+          gather_chunk<Real, Store, MODE, K, true>(a, ray, c, lane, v, bits, cs);
+        }
         if constexpr (LOGT) {
           float l = __shfl_sync(kFull, LTstart, c), lc = __shfl_sync(kFull, LCstart, c);
           scan_chunk_log<K>(v, l, lc, lane, Ts);
@@ -739,11 +804,7 @@ render_kernel(const RenderArgs<Real> a) {
               !(dv[0] != Real(0) || dv[1] != Real(0) || dv[2] != Real(0) || dv[3] != Real(0)))
             continue;
           Real nx, ny, nz;
-          if (PGB_COORDS_IN_SMEM) {
-            cs.get(k, lane, nx, ny, nz);
-          } else {
-            sample_coords(a, ray, (c * K + k) * kWarp + lane, nx, ny, nz);
-          }
+          cs.get(c, k, lane, nx, ny, nz);
           sample_scatter<Real, MODE>(a.g, a.grad, nx, ny, nz, dv, bk);
         }
       }
