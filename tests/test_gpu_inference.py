@@ -7,6 +7,7 @@ import torch
 
 import scenes
 from oracle import torch_port as tp
+import plenoxels_gb300 as pg
 from plenoxels_gb300.inference import visulize_3d_in_2d
 
 pytestmark = pytest.mark.gpu
@@ -32,3 +33,24 @@ def test_image_matches_reference_composition(do_threshold):
     diff = np.abs(img.astype(int) - ref.astype(int))
     assert diff.max() <= 1 and (diff > 0).mean() < 1e-3
     assert img.shape == (res, res, 4) and img.dtype == np.uint8
+
+
+def test_camera_images_are_the_renders_of_each_pixels_ray():
+    """render_camera_images: pixel (row, col) of camera c is the composited ray of the
+    uniforms (col / H, row / W) from that camera, started at near along its direction."""
+    import scenes
+    from oracle import torch_port as tp
+    side, S, H, near = 24, 64, 12, 2.0
+    grid = torch.from_numpy(scenes.make_grid(side, 3, 81, amp=(0.3, 3.0), negative_frac=0.02))
+    T = torch.from_numpy(scenes.make_cameras(2, 82))
+    pd, delta = scenes.points_distance(side), 4.0 / S
+    imgs = pg.inference.render_camera_images(grid.cuda(), T.cuda(), H, H, 0.691, near, delta, S, pd)
+    assert imgs.shape == (2, H, H, 4)
+    rows = torch.arange(H, device="cuda", dtype=torch.float32)
+    cols = torch.arange(H, device="cuda", dtype=torch.float32)
+    uv = torch.stack([(cols / H).expand(H, H), (rows / H)[:, None].expand(H, H)], -1).reshape(1, H * H, 2).cpu()
+    for c in range(2):
+        d, _ = tp.camera_rays(T[c:c + 1], 0.691, torch.zeros(1, H, H, 4), uv)
+        o = T[c, :3, 3] + near * d
+        ref = tp.render(grid, o, d, S, delta, tp.grid_min(grid.shape, pd), pd, "trilinear")
+        np.testing.assert_allclose(imgs[c].reshape(-1, 4).cpu().numpy(), ref.numpy(), rtol=1e-5, atol=2e-6)
