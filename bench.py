@@ -141,10 +141,10 @@ class Clocks:
 
 def unique_cells(pg, grid, T, imgs, W, seed, delta, pd):
     """Per-unit figures of the algorithmic byte count, from the kernels' own index math on
-    one step's rays (trilinear): distinct cells read by in-bounds samples (all of them, as
-    the reference reads them), distinct cells of the live samples (in bounds with
-    transmittance > 0: the samples behind an opaque one have weight 0 and gradient 0 and
-    need not be read), and the in-bounds and live shares of the samples."""
+    one step's rays (trilinear): (distinct cells read by in-bounds samples, as the
+    reference reads them; distinct cells of the live samples, in bounds with
+    transmittance > 0, which no exact implementation can skip; the in-bounds and live
+    shares of the samples)."""
     S, side = W["samples"], W["grid"]
     idx, inb, coords = pg.render.camera_sample_indices(
         grid, T, imgs, W["camera_angle_x"], W["rays"], seed, W["near"], delta, S, pd,
@@ -160,7 +160,7 @@ def unique_cells(pg, grid, T, imgs, W, seed, delta, pd):
     live_cells = int(torch.unique(lin[live.unsqueeze(-1).expand_as(lin)]).numel())
     shares = float(inb.float().mean()), float(live.float().mean())
     del idx, lin, coords, vals
-    return live_cells, all_cells, shares[0], shares[1]
+    return all_cells, live_cells, shares[0], shares[1]
 
 
 def reference_cpu_steps(W, steps, warmup, budget_s=None):
@@ -690,10 +690,13 @@ def main():
     # roofline of the fused kernel: algorithmic bytes per launch / its measured duration.
     # traffic: dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on
     # this workload under ncu
-    U, U_all, inb_frac, live_frac = unique_cells(pg, grid, T, imgs, W, 1000 * rank + args.warmup,
-                                                 delta, pd)
+    U, U_live, inb_frac, live_frac = unique_cells(pg, grid, T, imgs, W, 1000 * rank + args.warmup,
+                                                  delta, pd)
+    # U: distinct cells of the step's in-bounds samples (the cells the reference's
+    # algorithm reads); U_live: those of the live samples only (T > 0), the cells no exact
+    # implementation can skip
     alg_bytes = U * 16 + U * 16 + R * 60
-    alg_all = U_all * 16 + U_all * 16 + R * 60
+    alg_live = U_live * 16 + U_live * 16 + R * 60
     peak, peak_kind = _peaks()
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -701,11 +704,13 @@ def main():
                 "traffic_unit": "bytes per launch (ncu capture of this workload)",
                 "kernel": "render_kernel<trilinear,train>",
                 "kernel_ms": kern_ms, "unique_cells": U, "algorithmic_bytes": alg_bytes,
-                "unique_cells_definition": "distinct cells of the live samples (in bounds, "
-                                           "transmittance > 0); samples behind an opaque one "
-                                           "need not be read",
-                "unique_cells_all_samples": U_all, "algorithmic_bytes_all_samples": alg_all,
-                "frac_all_samples": alg_all / (kern_ms / 1e3) / 1e9 / peak,
+                "unique_cells_definition": "distinct cells read by the step's in-bounds samples "
+                                           "(all 8 corners), as the reference's algorithm reads them",
+                "unique_cells_live": U_live, "algorithmic_bytes_live": alg_live,
+                "frac_live": alg_live / (kern_ms / 1e3) / 1e9 / peak,
+                "live_definition": "cells of the live samples only (in bounds, transmittance > 0): "
+                                   "samples behind an opaque one have weight 0 and gradient 0, and "
+                                   "the kernel stops reading a ray after the chunk where T reaches 0",
                 "in_bounds_sample_share": inb_frac, "live_sample_share": live_frac,
                 "peak_kind": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured" else "fallback 6.8 TB/s",
                 "issued_gather_bytes": int(R * S * inb_frac * 8 * 16),

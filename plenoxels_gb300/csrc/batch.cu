@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
   __syncthreads();
   const int lane = threadIdx.x & (kWarp - 1);
   const int wib = threadIdx.x >> 5;
-  CoordStage<float, K> cs(smem_raw + tab_bytes, wib);
+  ChunkStage<float, K> cs(smem_raw + tab_bytes, wib);
 
   for (;;) {
     unsigned long long rr = 0;
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
         float t[4], nx, ny, nz;
         uint32_t b;
         if (batch_sample<Store, MODE>(ra, ray, sc, (c * K + k) * kWarp + lane, t, b, nx, ny, nz))
-          cs.put(k, lane, nx, ny, nz);
+          cs.put(c, k, lane, nx, ny, nz);
 #pragma unroll
         for (int kk = 0; kk < K; ++kk) {
           if (kk == k) {
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
       for (int k = 0; k < K; ++k) {
         float nx, ny, nz;
         if (batch_sample<Store, MODE>(ra, ray, sc, (c * K + k) * kWarp + lane, v[k], bits[k], nx, ny, nz))
-          cs.put(k, lane, nx, ny, nz);
+          cs.put(c, k, lane, nx, ny, nz);
       }
 #endif
     };
@@ -232,6 +232,8 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
       if (lane == c) Tstart = T;
       __syncwarp();
       gather(c);
+#pragma unroll
+      for (int k = 0; k < K; ++k) cs.put_vals(c, k, lane, v[k], bits[k]);
       T = scan_chunk<float, K>(v, T, lane, Ts);
 #pragma unroll
       for (int k = 0; k < K; ++k) {
@@ -262,7 +264,12 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
     for (int c = last; c >= 0; --c) {
       if (c != last) {
         __syncwarp();
-        gather(c);
+        if (ChunkStage<float, K>::holds(c, last)) {  // the chunk's values are still staged
+#pragma unroll
+          for (int k = 0; k < K; ++k) cs.get_vals(c, k, lane, v[k], bits[k]);
+        } else {
+          gather(c);
+        }
         scan_chunk<float, K>(v, __shfl_sync(kFull, Tstart, c), lane, Ts);
       }
       __syncwarp();
@@ -301,7 +308,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
             dv[0] = gpx[0] * w; dv[1] = gpx[1] * w; dv[2] = gpx[2] * w;
             dv[3] = tk * (G - S_after);
             has = dv[0] != 0.f || dv[1] != 0.f || dv[2] != 0.f || dv[3] != 0.f;
-            if (has) cs.get(k, lane, nx, ny, nz);
+            if (has) cs.get(c, k, lane, nx, ny, nz);
           }
           warp_merged_scatter<float>(ra.g, grad, has, nx, ny, nz, dv, bk, lane);
         } else if (bk != 0u) {
@@ -309,7 +316,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
           float dv[4] = {gpx[0] * w, gpx[1] * w, gpx[2] * w, tk * (G - S_after)};
           if (!(dv[0] != 0.f || dv[1] != 0.f || dv[2] != 0.f || dv[3] != 0.f)) continue;
           float nx, ny, nz;
-          cs.get(k, lane, nx, ny, nz);
+          cs.get(c, k, lane, nx, ny, nz);
           sample_scatter<float, MODE>(ra.g, grad, nx, ny, nz, dv, bk);
         }
       }
@@ -424,7 +431,7 @@ template <typename Store, int MODE, int K, bool MERGE>
 int launch_batch_k(const BatchArgs& a, int threads, cudaStream_t s) {
   const int warps = threads / kWarp;
   const size_t tab = (((size_t)a.num_scenes * sizeof(pgb_scene)) + 15) & ~(size_t)15;
-  const size_t smem = tab + (size_t)CoordStage<float, K>::kBytesPerWarp * warps;
+  const size_t smem = tab + (size_t)ChunkStage<float, K>::kBytesPerWarp * warps;
   auto kern = batch_train_kernel<Store, MODE, K, MERGE>;
   int dev = 0;
   cudaGetDevice(&dev);

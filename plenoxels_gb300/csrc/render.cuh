@@ -400,38 +400,15 @@ __device__ __forceinline__ void warp_merged_scatter(const GridP<Real>& g, Real* 
 #ifndef PGB_RENDER_MIN_BLOCKS_K1
 #define PGB_RENDER_MIN_BLOCKS_K1 3
 #endif
-#ifndef PGB_COORDS_IN_SMEM
-#define PGB_COORDS_IN_SMEM 1
-#endif
 
 constexpr int kRenderThreads = PGB_RENDER_THREADS;
-
-// Normalised coordinates of a warp's chunk kept for the reverse pass, so the adjoint does
-// not recompute the stratification hash and the three exact divisions: [3][K][32].
-template <typename Real, int K>
-struct CoordStage {
-  static constexpr int kBytesPerWarp = PGB_COORDS_IN_SMEM ? 3 * K * kWarp * (int)sizeof(Real) : 0;
-  Real* n;
-  __device__ __forceinline__ CoordStage(unsigned char* base, int warp)
-      : n(reinterpret_cast<Real*>(base + (size_t)warp * kBytesPerWarp)) {}
-  __device__ __forceinline__ void put(int k, int lane, Real x, Real y, Real z) {
-    n[(0 * K + k) * kWarp + lane] = x;
-    n[(1 * K + k) * kWarp + lane] = y;
-    n[(2 * K + k) * kWarp + lane] = z;
-  }
-  __device__ __forceinline__ void get(int k, int lane, Real& x, Real& y, Real& z) const {
-    x = n[(0 * K + k) * kWarp + lane];
-    y = n[(1 * K + k) * kWarp + lane];
-    z = n[(2 * K + k) * kWarp + lane];
-  }
-};
 
 // Chunks of 32 samples whose values the render kernel keeps per warp for its reverse pass.
 #ifndef PGB_STAGE_CHUNKS
 #define PGB_STAGE_CHUNKS 4
 #endif
 
-// The render kernel's per-warp shared-memory stage. It holds the normalised coordinates of
+// The per-warp shared-memory stage of the render and batched kernels. It holds the normalised coordinates of
 // the last M chunks, so the reverse pass does not recompute the stratification hash and
 // the exact divisions. With 32-sample chunks (K = 1, M = PGB_STAGE_CHUNKS) it also holds
 // their clamped values and clamp-pass bits, so the reverse pass reads the M - 1 chunks
