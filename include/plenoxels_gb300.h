@@ -93,6 +93,11 @@ typedef struct {
                                (0 for a batch of its own): ranks that split one batch of
                                explicit rays pass their share's offset, and every ray is
                                sampled as in the unsplit batch */
+  uint32_t* grad_marks;     /* optional device bitmap (NULL: none) of the gradient's 4-cell
+                               units: the backward and training entry points set bit
+                               (c/4) % 32 of word c/128 for every gradient cell c they write,
+                               so pgb_clear_marked can re-zero just those units. No
+                               counterpart in the reference. */
 } pgb_rays;
 
 /* ---- fused render path (scripts/train.py:142-156 composed with src/ray_sampling.py,
@@ -388,6 +393,13 @@ int pgb_remove_noise(float* cells, const int32_t dims[3], int32_t kernel_size, d
 /* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel: the
  * gradient zeroing of optimizer.zero_grad() (scripts/train.py:180) and of a fresh .grad. */
 int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream);
+/* Zeroes the gradient units marked in grad_marks (pgb_rays.grad_marks: 4 cells per unit,
+ * ceil(num_cells / 128) words) and clears the marks. A dense gradient buffer whose only
+ * writes since it was last zero are marked steps is zero again afterwards: the zeroing of
+ * optimizer.zero_grad() (scripts/train.py:180) restricted to the cells a step wrote. cell
+ * bytes: 16 (F32/BF16 grids' fp32 gradient) or 32 (F64). No counterpart in the reference. */
+int pgb_clear_marked(void* grad_cells, int32_t cell_bytes, int64_t num_cells, uint32_t* grad_marks,
+                     pgb_stream_t stream);
 
 /* The counter-based uniform in [0,1) used for stratification and in-kernel ray
  * generation, evaluated on the host: uniform(seed, a, b). Exact multiples of 2^-24. No

@@ -65,6 +65,7 @@ class PgbRays(Structure):
         ("log_transmittance", c_int32),
         ("chunk_samples", c_int32),
         ("first_ray", c_int64),
+        ("grad_marks", c_void_p),
     ]
 
 
@@ -131,6 +132,7 @@ _SIGNATURES = {
     "pgb_composite_fwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P]),
     "pgb_composite_bwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P, _P]),
     "pgb_fill_zero": (c_int32, [_P, c_int64, _P]),
+    "pgb_clear_marked": (c_int32, [_P, c_int32, c_int64, _P, _P]),
     "pgb_rgba_to_image": (c_int32, [_P, c_int32, _P, _P]),
     "pgb_splat_size": (c_int32, [POINTER(c_float), c_int32, POINTER(c_int32)]),
     "pgb_splat_preview": (c_int32, [_P, POINTER(c_int32), c_float, POINTER(c_float), c_float, c_int32, c_float,

@@ -45,6 +45,7 @@ int op_render_indices_f64(const RenderArgs<double>&, int, int64_t*, uint8_t*, cu
 int op_render_coords_f32(const RenderArgs<float>&, float*, cudaStream_t);
 int op_render_coords_f64(const RenderArgs<double>&, double*, cudaStream_t);
 int op_fill_zero(void*, int64_t, cudaStream_t);
+int op_clear_marked(void*, int, int64_t, uint32_t*, cudaStream_t);
 int op_rgba_to_image(const float*, int, uint8_t*, cudaStream_t);
 
 namespace {
@@ -378,6 +379,15 @@ int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream) {
   if (!ptr) return PGB_ERR_ARG;
   if (!aligned(ptr, 16)) return PGB_ERR_ALIGN;
   return op_fill_zero(ptr, bytes, stream);
+}
+
+int pgb_clear_marked(void* grad_cells, int32_t cell_bytes, int64_t num_cells, uint32_t* grad_marks,
+                     pgb_stream_t stream) {
+  if (num_cells < 0 || (cell_bytes != 16 && cell_bytes != 32)) return PGB_ERR_ARG;
+  if (num_cells == 0) return PGB_OK;
+  if (!grad_cells || !grad_marks) return PGB_ERR_ARG;
+  if (!aligned(grad_cells, 16) || !aligned(grad_marks, 4)) return PGB_ERR_ALIGN;
+  return op_clear_marked(grad_cells, cell_bytes, num_cells, grad_marks, stream);
 }
 
 float pgb_hash_uniform(uint64_t seed, uint64_t a, uint32_t b) {

@@ -588,6 +588,25 @@ __global__ void fill_zero_kernel(uint4* __restrict__ p, int64_t n16, uint8_t* __
   if (blockIdx.x == 0 && (int)threadIdx.x < tail_bytes) tail[threadIdx.x] = 0;
 }
 
+// One thread per mark word (32 units of 4 cells): zeroes each marked unit's cells
+// (`cells16` 16-byte slots per unit) and clears the word.
+__global__ void clear_marked_kernel(uint4* __restrict__ grad, int64_t total16, int cells16,
+                                    uint32_t* __restrict__ marks, int64_t words) {
+  PGB_FOR(w, words) {
+    uint32_t m = marks[w];
+    if (m == 0u) continue;
+    marks[w] = 0u;
+    while (m != 0u) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1u;
+      const int64_t first = (w * 32 + b) * (int64_t)cells16;
+#pragma unroll 4
+      for (int k = 0; k < cells16; ++k)
+        if (first + k < total16) grad[first + k] = make_uint4(0u, 0u, 0u, 0u);
+    }
+  }
+}
+
 }  // namespace
 
 // ================================================================ launchers
@@ -813,6 +832,15 @@ int op_render_indices_f64(const RenderArgs<double>& a, int mode, int64_t* idx, u
 
 int op_rgba_to_image(const float* rgba, int res, uint8_t* out, cudaStream_t s) {
   rgba_to_image_kernel<<<blocks_for((int64_t)res * res), kThreads, 0, s>>>(rgba, res, out);
+  return after_launch();
+}
+
+int op_clear_marked(void* grad, int cell_bytes, int64_t num_cells, uint32_t* marks, cudaStream_t s) {
+  const int64_t words = (num_cells + 127) / 128;
+  const int cells16 = 4 * cell_bytes / 16;  // 16-byte slots per 4-cell unit
+  const int64_t total16 = num_cells * cell_bytes / 16;
+  clear_marked_kernel<<<blocks_for(words), kThreads, 0, s>>>((uint4*)grad, total16, cells16, marks,
+                                                            words);
   return after_launch();
 }
 

@@ -70,6 +70,7 @@ struct RenderArgs {
   const Real* d_rgba;
   const Real* target;
   Real* grad;
+  uint32_t* grad_marks;  // optional: units of written gradient cells are marked here
   Real* loss_out;
   double* partials;
   unsigned* counter;
@@ -291,11 +292,19 @@ __device__ __forceinline__ void sample_value(const GridP<Real>& g, Real nx, Real
 #define PGB_SCATTER_ATTR __device__ __noinline__
 #endif
 
+// Marks the gradient unit of cell c (4 consecutive cells) in a bitmap of units: bit
+// (c / 4) % 32 of word c / 128.
+__device__ __forceinline__ void mark_unit(uint32_t* marks, uint64_t c) {
+  atomicOr(marks + (c >> 7), 1u << ((uint32_t)(c >> 2) & 31u));
+}
+
 // Scatter dL/dvalue of one sample into the dense gradient (the autograd replay of the
-// blend, the clamp mask and index_put accumulate).
+// blend, the clamp mask and index_put accumulate). marks (optional): the unit of every
+// written cell is marked.
 template <typename Real, int MODE>
 PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, Real ny,
-                                               Real nz, const Real dv[4], uint32_t bits) {
+                                     Real nz, const Real dv[4], uint32_t bits,
+                                     uint32_t* marks = nullptr) {
   if (bits == 0u) return;
   if (MODE == PGB_NEAREST) {
     Real gv[4];
@@ -303,6 +312,7 @@ PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, 
     for (int ch = 0; ch < 4; ++ch) gv[ch] = ((bits >> ch) & 1u) ? dv[ch] : Real(0);
     const uint64_t c = cell_index(g, (int)rround(nx), (int)rround(ny), (int)rround(nz));
     grad_add(grad, c, gv);
+    if (marks != nullptr) mark_unit(marks, c);
   } else {
     Corners<Real> q;
     trilinear_corners(g, nx, ny, nz, q);
@@ -327,7 +337,9 @@ PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, 
         const uint64_t row = (corner & 4) ? rowf : rowc;
         const int iy = (corner & 2) ? q.f[1] : q.c[1];
         const int iz = (corner & 1) ? q.f[2] : q.c[2];
-        grad_add(grad, (row + (uint64_t)iy) * (uint64_t)g.Z + (uint64_t)iz, gv);
+        const uint64_t cell = (row + (uint64_t)iy) * (uint64_t)g.Z + (uint64_t)iz;
+        grad_add(grad, cell, gv);
+        if (marks != nullptr) mark_unit(marks, cell);
       }
     }
   }
@@ -782,7 +794,7 @@ render_kernel(const RenderArgs<Real> a) {
             continue;
           Real nx, ny, nz;
           cs.get(c, k, lane, nx, ny, nz);
-          sample_scatter<Real, MODE>(a.g, a.grad, nx, ny, nz, dv, bk);
+          sample_scatter<Real, MODE>(a.g, a.grad, nx, ny, nz, dv, bk, a.grad_marks);
         }
       }
     }

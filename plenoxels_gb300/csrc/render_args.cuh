@@ -81,6 +81,7 @@ RenderArgs<Real> render_args(const pgb_grid* g, const pgb_rays* r) {
   a.stratified = r->stratified ? 1 : 0;
   a.strat_seed = r->seed;
   a.first_ray = r->first_ray;
+  a.grad_marks = r->grad_marks;
   a.term_thr = r->term_threshold;
   a.chunk_samples = r->chunk_samples;
   a.use_bg = r->use_background ? 1 : 0;

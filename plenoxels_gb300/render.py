@@ -36,7 +36,8 @@ def _transmittance(name: str) -> int:
 
 
 def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, seed, term_threshold,
-               cameras=None, background=None, log_t=0, chunk_samples=0, first_ray=0) -> PgbRays:
+               cameras=None, background=None, log_t=0, chunk_samples=0, first_ray=0,
+               grad_marks=None) -> PgbRays:
     r = PgbRays()
     r.origins = ptr(origins)
     r.dirs = ptr(dirs)
@@ -53,6 +54,7 @@ def _rays_desc(origins, dirs, num_rays, num_samples, delta_step, stratified, see
     r.log_transmittance = int(log_t)
     r.chunk_samples = int(chunk_samples)
     r.first_ray = int(first_ray)
+    r.grad_marks = ptr(grad_marks)
     return r
 
 
@@ -211,12 +213,18 @@ class FusedTrainStep:
     side stream while the current step's kernel runs (the 256 MiB fill of a 256^3 grid
     no longer sits on the critical path). A step's gradient then stays valid until the
     next step is launched; the buffer alternates, and ``grid.grad``/``self.grad`` follow.
+
+    zeroing="marked" re-zeroes a gradient buffer by clearing only the 4-cell units its
+    last step wrote (the kernel marks them in a bitmap of the buffer, pgb_clear_marked)
+    instead of writing the whole buffer. Every step still starts from an all-zero dense
+    gradient, provided the caller only reads the gradient buffers (an optimizer that
+    reads grid.grad, or zeroes it) and does not add into them.
     """
 
     def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
                  grid_min=None, clip=True, stratified=False, seed=0, term_threshold=0.0,
                  loss_weight=1.0, overlap_zero=False, beta=0.0, beta_eps=1e-4, background=None,
-                 transmittance="product", chunk_samples=0):
+                 transmittance="product", chunk_samples=0, zeroing="fill"):
         require_cuda(grid)
         if grid.dim() != 4 or grid.shape[-1] != 4 or not grid.is_contiguous():
             raise ValueError("grid must be a contiguous [X,Y,Z,4] tensor")
@@ -247,7 +255,13 @@ class FusedTrainStep:
             self._grads.append(torch.zeros(grid.shape, dtype=self.real, device=dev))
             self._side = torch.cuda.Stream(device=dev)
             self._zeroed = [None, None]  # event: buffer b is zero and free
+        if zeroing not in ("fill", "marked"):
+            raise ValueError(f"zeroing must be 'fill' or 'marked', got {zeroing!r}")
+        cells = grid.numel() // 4
+        self._marks = ([torch.zeros((cells + 127) // 128, dtype=torch.int32, device=dev)
+                        for _ in self._grads] if zeroing == "marked" else None)
         self._cur = 0
+        self._buf = 0  # index of the buffer the last launch wrote
         self.grad = self._grads[0]
         # losses[0]: loss_weight * MSE; losses[1]: the beta term (scripts/train.py:170-177)
         self.losses = torch.zeros(2, dtype=self.real, device=dev)
@@ -260,21 +274,29 @@ class FusedTrainStep:
         if self.grid.dtype == self.real and self.grid.requires_grad:
             self.grid.grad = self.grad
 
-    def _fill(self, buf, stream):
-        check(_lib.load().pgb_fill_zero(ptr(buf), buf.numel() * buf.element_size(),
-                                        stream.cuda_stream), "train step")
+    def _fill(self, b, stream):
+        buf = self._grads[b]
+        lib = _lib.load()
+        if self._marks is None:
+            check(lib.pgb_fill_zero(ptr(buf), buf.numel() * buf.element_size(), stream.cuda_stream),
+                  "train step")
+        else:
+            check(lib.pgb_clear_marked(ptr(buf), 4 * buf.element_size(), buf.numel() // 4,
+                                       ptr(self._marks[b]), stream.cuda_stream), "train step")
 
     def _gradient_for_step(self, zero_grad):
         main = torch.cuda.current_stream(self.grid.device)
         if not zero_grad:
             return self.grad
         if self._side is None:
-            self._fill(self.grad, main)
+            self._fill(0, main)
+            self._buf = 0
             return self.grad
         b = self._cur
         buf = self._grads[b]
+        self._buf = b
         if self._zeroed[b] is None:
-            self._fill(buf, main)
+            self._fill(b, main)
         else:
             main.wait_event(self._zeroed[b])
         # zero the other buffer for the next step, after everything already queued on the
@@ -283,7 +305,7 @@ class FusedTrainStep:
         ready = torch.cuda.Event()
         ready.record(main)
         self._side.wait_event(ready)
-        self._fill(self._grads[o], self._side)
+        self._fill(o, self._side)
         done = torch.cuda.Event()
         done.record(self._side)
         self._zeroed[o] = done
@@ -295,6 +317,8 @@ class FusedTrainStep:
     def _launch(self, rdesc, target, rgba_out, zero_grad):
         lib = _lib.load()
         grad = self._gradient_for_step(zero_grad)
+        if self._marks is not None:
+            rdesc.grad_marks = ptr(self._marks[self._buf])
         stream = torch.cuda.current_stream(self.grid.device)
         gdesc = _lib.make_grid(self.grid, self.grid_min, self.points_distance, self.mode, self.clip)
         ev = None

@@ -40,10 +40,11 @@ def test_struct_layout_matches_header(tmp_path):
         " offsetof(pgb_grid, points_distance), offsetof(pgb_grid, clip), offsetof(pgb_grid, mode));\n"
         'printf("%zu %zu %zu %zu\\n", sizeof(pgb_cameras), offsetof(pgb_cameras, camera_angle_x),'
         " offsetof(pgb_cameras, near), offsetof(pgb_cameras, seed));\n"
-        'printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(pgb_rays), offsetof(pgb_rays, num_rays),'
+        'printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(pgb_rays), offsetof(pgb_rays, num_rays),'
         " offsetof(pgb_rays, delta_step), offsetof(pgb_rays, seed), offsetof(pgb_rays, term_threshold),"
         " offsetof(pgb_rays, background), offsetof(pgb_rays, log_transmittance),"
-        " offsetof(pgb_rays, chunk_samples), offsetof(pgb_rays, first_ray));\n"
+        " offsetof(pgb_rays, chunk_samples), offsetof(pgb_rays, first_ray),"
+        " offsetof(pgb_rays, grad_marks));\n"
         'printf("%zu %zu %zu %zu %zu\\n", sizeof(pgb_scene), offsetof(pgb_scene, dims),'
         " offsetof(pgb_scene, origin), offsetof(pgb_scene, num_samples), offsetof(pgb_scene, delta_step));\n"
         "return 0;}\n")
@@ -58,7 +59,7 @@ def test_struct_layout_matches_header(tmp_path):
     assert c == [ctypes.sizeof(C), C.camera_angle_x.offset, C.near.offset, C.seed.offset]
     assert r == [ctypes.sizeof(R), R.num_rays.offset, R.delta_step.offset, R.seed.offset,
                  R.term_threshold.offset, R.background.offset, R.log_transmittance.offset,
-                 R.chunk_samples.offset, R.first_ray.offset]
+                 R.chunk_samples.offset, R.first_ray.offset, R.grad_marks.offset]
     sc = list(map(int, out[3].split()))
     P = _lib.PgbScene
     assert sc == [ctypes.sizeof(P), P.dims.offset, P.origin.offset, P.num_samples.offset,
@@ -124,6 +125,9 @@ def test_argument_validation_without_launch(lib):
                                 None) == _lib.PGB_ERR_ARG
     assert lib.pgb_wrap_indices(None, 3, None, None) == _lib.PGB_ERR_ARG
     assert lib.pgb_fill_zero(24, 16, None) == _lib.PGB_ERR_ALIGN
+    assert lib.pgb_clear_marked(16, 8, 64, 16, None) == _lib.PGB_ERR_ARG  # cell bytes
+    assert lib.pgb_clear_marked(None, 16, 64, 16, None) == _lib.PGB_ERR_ARG
+    assert lib.pgb_clear_marked(24, 16, 64, 16, None) == _lib.PGB_ERR_ALIGN
     # even_spread with a non-square ray count
     assert lib.pgb_generate_rays(16, 1, 10, ctypes.c_float(0.5), 16, 4, 4, None, 1, 16, 16, None,
                                  None) == _lib.PGB_ERR_ARG

@@ -389,3 +389,27 @@ def test_early_stop_behind_opaque_cells_is_exact(mode, dtype):
         torch.cuda.synchronize()
         np.testing.assert_allclose(float(got), float(loss), rtol=1e-5, err_msg=f"chunk {chunk}")
         _grad_close(step.grad, ref.grad)
+
+
+@pytest.mark.parametrize("mode", ["trilinear", "nearest"])
+@pytest.mark.parametrize("overlap", [False, True])
+def test_marked_zeroing_gives_the_dense_steps(mode, overlap):
+    """zeroing="marked" re-zeroes only the 4-cell units the buffer's last step wrote; over
+    steps on different rays (each touching other cells) every step must see an all-zero
+    buffer, so its gradient equals the dense-fill step's, zeros included; an accumulating
+    step (zero_grad=False) and the next zeroing clear its units too."""
+    grid = torch.from_numpy(scenes.make_grid(32, 4, 91, amp=(0.3, 3))).to(DEV)
+    T = torch.from_numpy(scenes.make_cameras(5, 92)).to(DEV)
+    imgs = torch.from_numpy(scenes.make_images(5, 16, 16, 93)).to(DEV)
+    pd, S = scenes.points_distance(32), 128
+    a = pg.FusedTrainStep(grid, pd, S, 4.0 / S, mode=mode, stratified=True, seed=3,
+                          overlap_zero=overlap, zeroing="marked")
+    b = pg.FusedTrainStep(grid, pd, S, 4.0 / S, mode=mode, stratified=True, seed=3)
+    for i in range(6):
+        acc = i == 3
+        la = a.step_cameras(T, imgs, 0.691, 700, 300 + i, near=2.0, zero_grad=not acc)
+        lb = b.step_cameras(T, imgs, 0.691, 700, 300 + i, near=2.0, zero_grad=not acc)
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(float(la), float(lb), rtol=1e-6)
+        # a cell left over from an earlier step would differ by that step's gradient
+        _grad_close(a.grad, b.grad, rel=1e-6)
