@@ -17,8 +17,8 @@ namespace pgb {
 namespace {
 
 // One ray per warp, so a call of at most PGB_NOALLOC_MAX_RAYS rays launches at most
-// kNoAllocMaxBlocks blocks, each writing one loss partial.
-constexpr int kNoAllocWarpsPerBlock = kRenderThreads / kWarp;
+// kNoAllocMaxBlocks blocks (of the smallest render block), each writing one loss partial.
+constexpr int kNoAllocWarpsPerBlock = kRenderMinThreads / kWarp;
 constexpr int kNoAllocMaxBlocks = PGB_NOALLOC_MAX_RAYS / kNoAllocWarpsPerBlock;
 static_assert(PGB_NOALLOC_MAX_RAYS % kNoAllocWarpsPerBlock == 0, "ray limit must fill whole blocks");
 static_assert(kNoAllocMaxBlocks * kNoAllocWarpsPerBlock <= kMaxTrainWarps,

@@ -588,21 +588,31 @@ __global__ void fill_zero_kernel(uint4* __restrict__ p, int64_t n16, uint8_t* __
   if (blockIdx.x == 0 && (int)threadIdx.x < tail_bytes) tail[threadIdx.x] = 0;
 }
 
-// One thread per mark word (32 units of 4 cells): zeroes each marked unit's cells
-// (`cells16` 16-byte slots per unit) and clears the word.
-__global__ void clear_marked_kernel(uint4* __restrict__ grad, int64_t total16, int cells16,
+// One warp per 32 mark words (a word marks 32 units of 4 cells). Each lane loads one word
+// and clears it; then for every word that had marks, the warp zeroes that word's units as
+// consecutive 16-byte slots (512 B per warp store, lanes of unmarked units skipping
+// theirs), so the stores stay coalesced however the marks are spread. `unit_shift` is
+// log2 of the 16-byte slots per unit (2 for fp32 cells, 3 for fp64).
+__global__ void clear_marked_kernel(uint4* __restrict__ grad, int64_t total16, int unit_shift,
                                     uint32_t* __restrict__ marks, int64_t words) {
-  PGB_FOR(w, words) {
-    uint32_t m = marks[w];
-    if (m == 0u) continue;
-    marks[w] = 0u;
-    while (m != 0u) {
-      const int b = __ffs(m) - 1;
-      m &= m - 1u;
-      const int64_t first = (w * 32 + b) * (int64_t)cells16;
-#pragma unroll 4
-      for (int k = 0; k < cells16; ++k)
-        if (first + k < total16) grad[first + k] = make_uint4(0u, 0u, 0u, 0u);
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int slots = 32 << unit_shift;  // 16-byte slots under one word
+  for (int64_t base = warp * 32; base < words; base += warps * 32) {
+    const int64_t w = base + lane;
+    const uint32_t mine = w < words ? marks[w] : 0u;
+    if (mine != 0u) marks[w] = 0u;
+    uint32_t pending = __ballot_sync(0xffffffffu, mine != 0u);
+    while (pending != 0u) {
+      const int src = __ffs(pending) - 1;
+      pending &= pending - 1u;
+      const uint32_t m = __shfl_sync(0xffffffffu, mine, src);
+      const int64_t first = (base + src) * (int64_t)slots;
+      for (int s = lane; s < slots; s += 32) {
+        const int64_t at = first + s;
+        if (((m >> (s >> unit_shift)) & 1u) && at < total16) grad[at] = make_uint4(0u, 0u, 0u, 0u);
+      }
     }
   }
 }
@@ -837,10 +847,11 @@ int op_rgba_to_image(const float* rgba, int res, uint8_t* out, cudaStream_t s) {
 
 int op_clear_marked(void* grad, int cell_bytes, int64_t num_cells, uint32_t* marks, cudaStream_t s) {
   const int64_t words = (num_cells + 127) / 128;
-  const int cells16 = 4 * cell_bytes / 16;  // 16-byte slots per 4-cell unit
+  const int unit_shift = cell_bytes == 32 ? 3 : 2;  // log2 of 16-byte slots per 4-cell unit
   const int64_t total16 = num_cells * cell_bytes / 16;
-  clear_marked_kernel<<<blocks_for(words), kThreads, 0, s>>>((uint4*)grad, total16, cells16, marks,
-                                                            words);
+  // one thread per word: each warp takes 32 consecutive words
+  clear_marked_kernel<<<blocks_for(words), kThreads, 0, s>>>((uint4*)grad, total16, unit_shift,
+                                                            marks, words);
   return after_launch();
 }
 

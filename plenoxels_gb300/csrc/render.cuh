@@ -321,8 +321,16 @@ PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, 
     // corner weights, corner order of src/grid_functions.py:16-24
     const Real wyz[4] = {wy * wz, wy * uz, uy * wz, uy * uz};
     const uint64_t rowc = (uint64_t)q.c[0] * (uint64_t)g.Y, rowf = (uint64_t)q.f[0] * (uint64_t)g.Y;
+    // marks of the two z-neighbour corners (same x, y) mostly fall in one word: OR them
+    // together and flush once per pair
+    uint64_t mark_word = 0;
+    uint32_t mark_bits = 0u;
 #pragma unroll
     for (int corner = 0; corner < 8; ++corner) {
+      if (marks != nullptr && (corner & 1) == 0 && mark_bits != 0u) {
+        atomicOr(marks + mark_word, mark_bits);
+        mark_bits = 0u;
+      }
       const Real wc = ((corner & 4) ? ux : wx) * wyz[corner & 3];
       const uint32_t cb = bits >> (4 * corner);
       if ((cb & 0xfu) == 0u) continue;
@@ -339,9 +347,19 @@ PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, 
         const int iz = (corner & 1) ? q.f[2] : q.c[2];
         const uint64_t cell = (row + (uint64_t)iy) * (uint64_t)g.Z + (uint64_t)iz;
         grad_add(grad, cell, gv);
-        if (marks != nullptr) mark_unit(marks, cell);
+        if (marks != nullptr) {
+          const uint64_t word = cell >> 7;
+          const uint32_t bit = 1u << ((uint32_t)(cell >> 2) & 31u);
+          if (mark_bits != 0u && word != mark_word) {
+            atomicOr(marks + mark_word, mark_bits);
+            mark_bits = 0u;
+          }
+          mark_word = word;
+          mark_bits |= bit;
+        }
       }
     }
+    if (marks != nullptr && mark_bits != 0u) atomicOr(marks + mark_word, mark_bits);
   }
 }
 
@@ -407,13 +425,24 @@ __device__ __forceinline__ void warp_merged_scatter(const GridP<Real>& g, Real* 
 #ifndef PGB_RENDER_MIN_BLOCKS_NEAREST
 #define PGB_RENDER_MIN_BLOCKS_NEAREST 4
 #endif
-// Trilinear lookup with 32-sample chunks: 3 blocks per SM (80 registers, a 32-byte spill)
-// measured 0.127 ms per step against 0.133 ms at 2 blocks (256^3, 8192 rays x 256).
+// Trilinear lookup with 32-sample chunks: 24 resident warps per SM (80 registers, a
+// 32-byte spill) measured 0.127 ms per step against 0.133 ms at 16 (256^3, 8192 rays x
+// 256). Its blocks are 128 threads: a block holds its SM slot until its slowest ray ends,
+// and rays end at very different depths once they stop behind opaque cells, so smaller
+// blocks free slots sooner (kernel 0.094 ms against 0.098 ms at 256 threads; 64 threads
+// took 0.102 ms). Nearest lookup measured best at 256 threads.
+#ifndef PGB_RENDER_THREADS_K1
+#define PGB_RENDER_THREADS_K1 128
+#endif
 #ifndef PGB_RENDER_MIN_BLOCKS_K1
-#define PGB_RENDER_MIN_BLOCKS_K1 3
+#define PGB_RENDER_MIN_BLOCKS_K1 (3 * 256 / PGB_RENDER_THREADS_K1)
 #endif
 
 constexpr int kRenderThreads = PGB_RENDER_THREADS;
+constexpr int kRenderThreadsK1 = PGB_RENDER_THREADS_K1;
+// the smallest block of any render launch (it bounds the number of blocks per ray count)
+constexpr int kRenderMinThreads = kRenderThreads < kRenderThreadsK1 ? kRenderThreads
+                                                                     : kRenderThreadsK1;
 
 // Chunks of 32 samples whose values the render kernel keeps per warp for its reverse pass.
 #ifndef PGB_STAGE_CHUNKS
@@ -593,6 +622,11 @@ constexpr int render_smem_bytes(int warps_per_block) {
 }
 
 template <int MODE, int K>
+constexpr int render_threads() {
+  return MODE != PGB_NEAREST && K == 1 ? kRenderThreadsK1 : kRenderThreads;
+}
+
+template <int MODE, int K>
 constexpr int render_min_blocks() {
   return MODE == PGB_NEAREST ? PGB_RENDER_MIN_BLOCKS_NEAREST
                              : (K == 1 ? PGB_RENDER_MIN_BLOCKS_K1 : PGB_RENDER_MIN_BLOCKS);
@@ -601,7 +635,7 @@ constexpr int render_min_blocks() {
 // LOGT: transmittance as the compensated log-sum (scan_chunk_log, fp32 only) instead of
 // the reference's product scan.
 template <typename Real, typename Store, int MODE, int K, int PHASE, bool LOGT = false>
-__global__ void __launch_bounds__(kRenderThreads, (render_min_blocks<MODE, K>()))
+__global__ void __launch_bounds__((render_threads<MODE, K>()), (render_min_blocks<MODE, K>()))
 render_kernel(const RenderArgs<Real> a) {
   static_assert(!LOGT || sizeof(Real) == 4, "log-sum transmittance is an fp32 form");
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -627,6 +661,7 @@ render_kernel(const RenderArgs<Real> a) {
   constexpr uint32_t kAlphaBits = MODE == PGB_NEAREST ? 0x8u : 0x88888888u;
   // beta_w / (R*S) * (1 + 2 eps): the numerator of 1/(alpha+eps) + 1/(1-alpha+eps)
   const Real beta_scale = (Real)(a.beta_w * a.inv_samples * (1.0 + 2.0 * (double)a.beta_eps));
+  const Real grad_scale = (Real)(2.0 * a.loss_w * a.inv_count);  // d(weighted MSE)/d pixel
   __shared__ double s_part[32];  // per-warp loss partials (training phase)
   __shared__ double s_part_beta[32];
   __shared__ unsigned s_done;    // warps of this block that finished (training phase)
@@ -720,14 +755,15 @@ render_kernel(const RenderArgs<Real> a) {
 #pragma unroll
       for (int ch = 0; ch < 4; ++ch) gpx[ch] = a.d_rgba[4 * r + ch];
     } else {
-      double sq = 0.0;
+      // the ray's squared error in Real (4 terms), accumulated over rays in double
+      Real sq = Real(0);
 #pragma unroll
       for (int ch = 0; ch < 4; ++ch) {
         const Real diff = px[ch] - ray.tgt[ch];
-        sq += (double)diff * (double)diff;
-        gpx[ch] = (Real)(2.0 * a.loss_w * a.inv_count) * diff;
+        sq += diff * diff;
+        gpx[ch] = grad_scale * diff;
       }
-      if (lane == 0) loss_lane += sq;
+      if (lane == 0) loss_lane += (double)sq;
       if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = pick4(px, lane);
     }
     if (a.use_bg)  // d(rgb + (1 - A) bg)/dA = -bg
@@ -806,7 +842,7 @@ render_kernel(const RenderArgs<Real> a) {
     // the last block sums the blocks in block order
     const int wib = threadIdx.x >> 5;
     unsigned last_warp = 0;
-    beta_lane = warp_sum(beta_lane);
+    if (with_beta) beta_lane = warp_sum(beta_lane);
     if (lane == 0) {
       s_part[wib] = loss_lane;
       s_part_beta[wib] = beta_lane;
@@ -835,21 +871,26 @@ render_kernel(const RenderArgs<Real> a) {
         // partials were written by other blocks before their ticket)
         double sum = 0.0, bsum = 0.0;
         for (unsigned i0 = lane; i0 < gridDim.x; i0 += 8 * kWarp) {
-          double p[8], q[8];
+          double p[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             const unsigned i = i0 + u * kWarp;
             p[u] = i < gridDim.x ? __ldcg(a.partials + i) : 0.0;
-            q[u] = (with_beta && i < gridDim.x) ? __ldcg(a.partials_beta + i) : 0.0;
           }
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            sum += p[u];
-            bsum += q[u];
+          for (int u = 0; u < 8; ++u) sum += p[u];
+          if (with_beta) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const unsigned i = i0 + u * kWarp;
+              p[u] = i < gridDim.x ? __ldcg(a.partials_beta + i) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) bsum += p[u];
           }
         }
         sum = warp_sum(sum);
-        bsum = warp_sum(bsum);
+        if (with_beta) bsum = warp_sum(bsum);
         if (lane == 0) {
           a.loss_out[0] = (Real)(a.loss_w * sum * a.inv_count);
           if (with_beta) a.loss_out[1] = (Real)(a.beta_w * bsum * a.inv_samples);

@@ -413,3 +413,35 @@ def test_marked_zeroing_gives_the_dense_steps(mode, overlap):
         np.testing.assert_allclose(float(la), float(lb), rtol=1e-6)
         # a cell left over from an earlier step would differ by that step's gradient
         _grad_close(a.grad, b.grad, rel=1e-6)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+@pytest.mark.parametrize("num_cells", [1000, 128 * 40 + 3, 256 * 1024 + 130])
+def test_clear_marked_zeroes_exactly_the_marked_units(dtype, num_cells):
+    """pgb_clear_marked zeroes the cells of every marked 4-cell unit (bit (c/4)%32 of word
+    c/128), leaves every other cell as it was, stops at num_cells (a ragged last unit and
+    word) and leaves the bitmap all zero; words with every bit set, none, and random
+    sparse bits."""
+    lib = _lib.load()
+    rng = np.random.default_rng(num_cells)
+    words = (num_cells + 127) // 128
+    units = (num_cells + 3) // 4
+    bits = rng.random(words * 32) < 0.05
+    bits[: 32 * min(3, words)] = True  # full words at the start
+    bits[32 * 5: 32 * 7] = False       # empty words
+    bits[units - 1] = True             # the ragged last unit
+    bits[units:] = False               # no unit past the cells
+    words_np = np.packbits(bits.reshape(words, 32)[:, ::-1], axis=1, bitorder="big")
+    marks_np = words_np.view(">u4").astype(np.uint32).reshape(words)
+    grad = torch.arange(1, num_cells * 4 + 1, dtype=dtype, device=DEV).reshape(num_cells, 4)
+    marks = torch.from_numpy(marks_np.view(np.int32)).to(DEV)
+    before = grad.clone()
+    cell_bytes = 4 * grad.element_size()
+    st = lib.pgb_clear_marked(grad.data_ptr(), cell_bytes, num_cells, marks.data_ptr(),
+                              torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    torch.cuda.synchronize()
+    cell_marked = torch.from_numpy(np.repeat(bits[:units], 4)[:num_cells]).to(DEV)
+    expect = torch.where(cell_marked[:, None], torch.zeros_like(before), before)
+    assert torch.equal(grad, expect)
+    assert int(marks.abs().sum()) == 0
