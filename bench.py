@@ -416,7 +416,7 @@ def batched_leg(pg, dev, steps=30, seed=11, num_scenes=64):
             "chosen_tile": f"K{step.tiles[0]}_t{step.tiles[1]}" + ("_merge" if step.tiles[2] else ""),
             "chosen_brick_cells": 1 << step.brick_log2,
             "note": "BF16 cells, occupancy-masked fp32 gradients, early termination at T<1e-4, "
-                    "CUDA-graph replay of zeroing + one persistent launch; same rays every step"}
+                    "CUDA-graph replay of zeroing + one persistent launch + the ordered loss sum; same rays every step"}
 
 
 def full_step_leg(pg, grid, T, imgs, W, dev, steps, warmup):

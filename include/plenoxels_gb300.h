@@ -219,7 +219,8 @@ int pgb_batch_zero_grads(const pgb_scene* scenes, int32_t num_scenes, int64_t ma
  * back NaN). merge_updates = 1 (trilinear) sums the updates that lanes of a warp make to
  * the same cell before the atomic adds (a tile choice: same gradient, summed in another
  * order). workspace: pgb_batch_workspace_bytes(R), zeroed once before first use; the
- * kernel leaves its counters zeroed. */
+ * call's two kernels (the persistent step, then the ordered loss sum) leave their
+ * counters zeroed. */
 int64_t pgb_batch_workspace_bytes(int64_t num_rays);
 int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, int32_t mode,
                     int32_t clip, const float* origins, const float* dirs, const float* target,

@@ -72,8 +72,15 @@ struct BatchArgs {
   float* loss_out;
   unsigned long long* work;  // ray queue head
   unsigned* ticket;          // finished blocks
-  double* ray_loss;          // [R] squared error per ray
+  float* ray_loss;           // [R] squared error per ray
 };
+
+// Workspace: the queue head (8 B), the finished-block ticket (4 B) and the loss sum's
+// ticket (4 B) in the first 64 B, then the loss sum's block partials, then one float per
+// ray.
+constexpr int kLossBlocks = 1024;
+constexpr int64_t kLossPartialsOffset = 64;
+constexpr int64_t kRayLossOffset = kLossPartialsOffset + 8 * kLossBlocks;
 
 __device__ __forceinline__ bool brick_clear(const pgb_scene& sc, float nx, float ny, float nz) {
   if (sc.bricks == nullptr) return false;
@@ -148,11 +155,11 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
     const int words = (int)((size_t)a.num_scenes * sizeof(pgb_scene) / 4);
     for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
   }
-  __shared__ unsigned s_last;
   __syncthreads();
   const int lane = threadIdx.x & (kWarp - 1);
   const int wib = threadIdx.x >> 5;
   ChunkStage<float, K> cs(smem_raw + tab_bytes, wib);
+  const float grad_scale = (float)(2.0 * a.loss_w * a.inv_count);  // d(weighted MSE)/d pixel
 
   for (;;) {
     unsigned long long rr = 0;
@@ -162,7 +169,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
     const int64_t r = (int64_t)rr;
     const int sid = a.ray_scene[r];
     if ((unsigned)sid >= (unsigned)a.num_scenes) {  // not a scene of this batch: no work
-      if (lane == 0) a.ray_loss[r] = 0.0;
+      if (lane == 0) a.ray_loss[r] = 0.f;
       if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = 0.f;
       continue;
     }
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
 
     const int nchunks = (ra.S + kWarp * K - 1) / (kWarp * K);
     if (nchunks > kWarp) {  // a chunk start per lane: more chunks are not supported
-      if (lane == 0) a.ray_loss[r] = __longlong_as_double(0x7ff8000000000000ll);  // NaN loss
+      if (lane == 0) a.ray_loss[r] = __int_as_float(0x7fc00000);  // NaN loss
       if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = __int_as_float(0x7fc00000);
       continue;
     }
@@ -250,12 +257,12 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
 #pragma unroll
     for (int ch = 0; ch < 4; ++ch) px[ch] = warp_sum(acc[ch]);
     float gpx[4];
-    double sq = 0.0;
+    float sq = 0.f;
 #pragma unroll
     for (int ch = 0; ch < 4; ++ch) {
       const float diff = px[ch] - ray.tgt[ch];
-      sq += (double)diff * (double)diff;
-      gpx[ch] = (float)(2.0 * a.loss_w * a.inv_count) * diff;
+      sq += diff * diff;
+      gpx[ch] = grad_scale * diff;
     }
     if (lane == 0) a.ray_loss[r] = sq;
     if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = pick4(px, lane);
@@ -323,29 +330,58 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
     }
   }
 
-  // the last block to finish sums the per-ray losses in ray order and resets the queue
+  // the last block to finish resets the queue (ray_loss_sum_kernel, launched next, sums
+  // the per-ray losses)
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    s_last = atomicAdd(a.ticket, 1u) == gridDim.x - 1u;
-  }
-  __syncthreads();
-  if (s_last) {
-    __threadfence();
-    __shared__ double red[kBatchMaxThreads];
-    double sum = 0.0;
-    for (int64_t i = threadIdx.x; i < a.R; i += blockDim.x) sum += ((volatile double*)a.ray_loss)[i];
-    red[threadIdx.x] = sum;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      a.loss_out[0] = (float)(a.loss_w * red[0] * a.inv_count);
+    if (atomicAdd(a.ticket, 1u) == gridDim.x - 1u) {
       *a.work = 0ull;
       *a.ticket = 0u;
     }
+  }
+}
+
+// The weighted MSE from the per-ray squared errors, in a fixed order: block b adds rays
+// [b * seg, (b + 1) * seg) (thread-strided, then a tree), and the last block to finish
+// adds the block sums in block order. Every SM takes a share of the fp64 adds (GB300's
+// fp64 rate is low), instead of one block adding all rays.
+__global__ void __launch_bounds__(256) ray_loss_sum_kernel(const float* __restrict__ ray_loss,
+                                                           int64_t R, int64_t seg,
+                                                           double* __restrict__ partials,
+                                                           unsigned* ticket, float* loss_out,
+                                                           double loss_w, double inv_count) {
+  __shared__ double red[256];
+  __shared__ unsigned s_last;
+  const int64_t lo = (int64_t)blockIdx.x * seg;
+  const int64_t hi = lo + seg < R ? lo + seg : R;
+  double sum = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) sum += (double)ray_loss[i];
+  red[threadIdx.x] = sum;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = red[0];
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1u;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double t = 0.0;
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) t += __ldcg(partials + i);
+  red[threadIdx.x] = t;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    loss_out[0] = (float)(loss_w * red[0] * inv_count);
+    *ticket = 0u;
   }
 }
 
@@ -479,7 +515,7 @@ using namespace pgb;
 extern "C" {
 
 int64_t pgb_batch_workspace_bytes(int64_t num_rays) {
-  return 64 + 8 * std::max<int64_t>(num_rays, 1);
+  return kRayLossOffset + 4 * std::max<int64_t>(num_rays, 1);
 }
 
 int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, int32_t mode,
@@ -516,14 +552,24 @@ int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, 
   a.loss_out = loss_out;
   a.work = reinterpret_cast<unsigned long long*>(workspace);
   a.ticket = reinterpret_cast<unsigned*>((char*)workspace + 8);
-  a.ray_loss = reinterpret_cast<double*>((char*)workspace + 64);
+  a.ray_loss = reinterpret_cast<float*>((char*)workspace + kRayLossOffset);
   const int merge = merge_updates ? 1 : 0;
+  int st;
   if (dtype == PGB_BF16)
-    return mode == PGB_NEAREST
-               ? launch_batch_m<__nv_bfloat16, PGB_NEAREST>(a, K, threads, merge, stream)
-               : launch_batch_m<__nv_bfloat16, PGB_TRILINEAR>(a, K, threads, merge, stream);
-  return mode == PGB_NEAREST ? launch_batch_m<float, PGB_NEAREST>(a, K, threads, merge, stream)
+    st = mode == PGB_NEAREST
+             ? launch_batch_m<__nv_bfloat16, PGB_NEAREST>(a, K, threads, merge, stream)
+             : launch_batch_m<__nv_bfloat16, PGB_TRILINEAR>(a, K, threads, merge, stream);
+  else
+    st = mode == PGB_NEAREST ? launch_batch_m<float, PGB_NEAREST>(a, K, threads, merge, stream)
                              : launch_batch_m<float, PGB_TRILINEAR>(a, K, threads, merge, stream);
+  if (st != PGB_OK) return st;
+  // about 1024 rays per block, at most kLossBlocks blocks
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(kLossBlocks, (num_rays + 1023) / 1024));
+  const int64_t seg = (num_rays + blocks - 1) / blocks;
+  ray_loss_sum_kernel<<<(unsigned)blocks, 256, 0, stream>>>(
+      a.ray_loss, num_rays, seg, reinterpret_cast<double*>((char*)workspace + kLossPartialsOffset),
+      reinterpret_cast<unsigned*>((char*)workspace + 12), loss_out, a.loss_w, a.inv_count);
+  return after_launch();
 }
 
 int pgb_pack_mask(const uint8_t* mask, int64_t count, uint32_t* bits_out, pgb_stream_t stream) {
