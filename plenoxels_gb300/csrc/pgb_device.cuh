@@ -152,4 +152,87 @@ __device__ __forceinline__ Real warp_sum(Real x) {
   return x;
 }
 
+// A running sum of loss terms kept in an 8-byte slot. For fp64 kernels a plain double.
+// For fp32 kernels an unevaluated pair hi + lo of floats, each term added with Knuth's
+// TwoSum (the rounding error of hi + x is exact and goes to lo), ~48 bits in all: the
+// sums stay in fp32 arithmetic, since GB300's fp64 rate is a small fraction of its fp32
+// rate and the loss reductions sit on the kernels' critical path.
+template <typename Real>
+struct LossSum {
+  double v = 0.0;
+  __device__ __forceinline__ void add(double x) { v += x; }
+  __device__ __forceinline__ void add(const LossSum& o) { v += o.v; }
+  __device__ __forceinline__ double value() const { return v; }
+  __device__ __forceinline__ void store(double* slot) const { *slot = v; }
+  __device__ __forceinline__ void store_volatile(double* slot) const {
+    *(volatile double*)slot = v;
+  }
+  __device__ __forceinline__ static LossSum load_volatile(const double* slot) {
+    LossSum s;
+    s.v = *(const volatile double*)slot;
+    return s;
+  }
+  __device__ __forceinline__ static LossSum load_cg(const double* slot) {
+    LossSum s;
+    s.v = __ldcg(slot);
+    return s;
+  }
+  __device__ __forceinline__ LossSum shfl_xor(int d) const {
+    LossSum s;
+    s.v = __shfl_xor_sync(kFull, v, d);
+    return s;
+  }
+};
+
+template <>
+struct LossSum<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = hi + x;
+    const float b = s - hi;
+    lo += (hi - (s - b)) + (x - b);
+    hi = s;
+  }
+  __device__ __forceinline__ void add(const LossSum& o) {
+    add(o.hi);
+    lo += o.lo;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ void store(double* slot) const {
+    *reinterpret_cast<float2*>(slot) = make_float2(hi, lo);
+  }
+  __device__ __forceinline__ void store_volatile(double* slot) const {
+    volatile float* q = reinterpret_cast<volatile float*>(slot);
+    q[0] = hi;
+    q[1] = lo;
+  }
+  __device__ __forceinline__ static LossSum load_volatile(const double* slot) {
+    const volatile float* q = reinterpret_cast<const volatile float*>(slot);
+    LossSum s;
+    s.hi = q[0];
+    s.lo = q[1];
+    return s;
+  }
+  __device__ __forceinline__ static LossSum load_cg(const double* slot) {
+    const float2 p = __ldcg(reinterpret_cast<const float2*>(slot));
+    LossSum s;
+    s.hi = p.x;
+    s.lo = p.y;
+    return s;
+  }
+  __device__ __forceinline__ LossSum shfl_xor(int d) const {
+    LossSum s;
+    s.hi = __shfl_xor_sync(kFull, hi, d);
+    s.lo = __shfl_xor_sync(kFull, lo, d);
+    return s;
+  }
+};
+
+template <typename Real>
+__device__ __forceinline__ LossSum<Real> warp_sum(LossSum<Real> x) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) x.add(x.shfl_xor(d));
+  return x;
+}
+
 }  // namespace pgb

@@ -646,8 +646,8 @@ render_kernel(const RenderArgs<Real> a) {
   const int64_t nw = (int64_t)gridDim.x * warps_per_block;
   const int nchunks = (a.S + kWarp * K - 1) / (kWarp * K);
   ChunkStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
-  double loss_lane = 0.0;
-  double beta_lane = 0.0;
+  LossSum<Real> loss_lane;  // lane 0: squared errors of the warp's rays
+  LossSum<Real> beta_lane;  // per lane: beta terms of its samples
   const bool with_beta = PHASE == kTrain && a.beta_w != 0.0;
   // Exact early stop. With alpha clamped to [0,1], T is exactly 0 only behind an opaque
   // sample z (alpha_z = 1) or after an underflow, and every later sample then has weight
@@ -719,7 +719,7 @@ render_kernel(const RenderArgs<Real> a) {
             bsum += log(al + e) - log(Real(1) - al + e);
           }
         }
-        beta_lane += (double)bsum;
+        beta_lane.add(bsum);
       }
       last = c;
       if (stop_at_zero) {
@@ -763,7 +763,7 @@ render_kernel(const RenderArgs<Real> a) {
         sq += diff * diff;
         gpx[ch] = grad_scale * diff;
       }
-      if (lane == 0) loss_lane += (double)sq;
+      if (lane == 0) loss_lane.add(sq);
       if (a.rgba_out != nullptr && lane < 4) a.rgba_out[4 * r + lane] = pick4(px, lane);
     }
     if (a.use_bg)  // d(rgb + (1 - A) bg)/dA = -bg
@@ -844,8 +844,8 @@ render_kernel(const RenderArgs<Real> a) {
     unsigned last_warp = 0;
     if (with_beta) beta_lane = warp_sum(beta_lane);
     if (lane == 0) {
-      s_part[wib] = loss_lane;
-      s_part_beta[wib] = beta_lane;
+      loss_lane.store_volatile(&s_part[wib]);
+      beta_lane.store_volatile(&s_part_beta[wib]);
       __threadfence_block();
       last_warp = atomicAdd(&s_done, 1u) == (unsigned)warps_per_block - 1u;
     }
@@ -854,13 +854,13 @@ render_kernel(const RenderArgs<Real> a) {
       unsigned last_block = 0;
       if (lane == 0) {
         __threadfence_block();
-        double sum = 0.0, bsum = 0.0;
+        LossSum<Real> sum, bsum;
         for (int i = 0; i < warps_per_block; ++i) {
-          sum += ((volatile double*)s_part)[i];
-          bsum += ((volatile double*)s_part_beta)[i];
+          sum.add(LossSum<Real>::load_volatile(&s_part[i]));
+          bsum.add(LossSum<Real>::load_volatile(&s_part_beta[i]));
         }
-        a.partials[blockIdx.x] = sum;
-        if (with_beta) a.partials_beta[blockIdx.x] = bsum;
+        sum.store(a.partials + blockIdx.x);
+        if (with_beta) bsum.store(a.partials_beta + blockIdx.x);
         __threadfence();
         last_block = atomicAdd(a.counter, 1u) == gridDim.x - 1u;
       }
@@ -869,31 +869,31 @@ render_kernel(const RenderArgs<Real> a) {
         __threadfence();
         // block partials in block order, eight loads in flight per lane (L2 reads: the
         // partials were written by other blocks before their ticket)
-        double sum = 0.0, bsum = 0.0;
+        LossSum<Real> sum, bsum;
         for (unsigned i0 = lane; i0 < gridDim.x; i0 += 8 * kWarp) {
-          double p[8];
+          LossSum<Real> p[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             const unsigned i = i0 + u * kWarp;
-            p[u] = i < gridDim.x ? __ldcg(a.partials + i) : 0.0;
+            if (i < gridDim.x) p[u] = LossSum<Real>::load_cg(a.partials + i);
           }
 #pragma unroll
-          for (int u = 0; u < 8; ++u) sum += p[u];
+          for (int u = 0; u < 8; ++u) sum.add(p[u]);
           if (with_beta) {
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
               const unsigned i = i0 + u * kWarp;
-              p[u] = i < gridDim.x ? __ldcg(a.partials_beta + i) : 0.0;
+              if (i < gridDim.x) p[u] = LossSum<Real>::load_cg(a.partials_beta + i);
             }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) bsum += p[u];
+            for (int u = 0; u < 8; ++u) bsum.add(p[u]);
           }
         }
         sum = warp_sum(sum);
         if (with_beta) bsum = warp_sum(bsum);
         if (lane == 0) {
-          a.loss_out[0] = (Real)(a.loss_w * sum * a.inv_count);
-          if (with_beta) a.loss_out[1] = (Real)(a.beta_w * bsum * a.inv_samples);
+          a.loss_out[0] = (Real)(a.loss_w * sum.value() * a.inv_count);
+          if (with_beta) a.loss_out[1] = (Real)(a.beta_w * bsum.value() * a.inv_samples);
           *a.counter = 0u;
         }
       }
