@@ -588,33 +588,13 @@ __global__ void fill_zero_kernel(uint4* __restrict__ p, int64_t n16, uint8_t* __
   if (blockIdx.x == 0 && (int)threadIdx.x < tail_bytes) tail[threadIdx.x] = 0;
 }
 
-// One warp per 32 mark words (a word marks 32 units of 4 cells). Each lane loads one word
-// and clears it; then for every word that had marks, the warp zeroes that word's units as
-// consecutive 16-byte slots (512 B per warp store, lanes of unmarked units skipping
-// theirs), so the stores stay coalesced however the marks are spread. `unit_shift` is
-// log2 of the 16-byte slots per unit (2 for fp32 cells, 3 for fp64).
+// Zeroes the marked units of a gradient buffer and clears the marks (clear_marked_warp),
+// every warp of the grid taking rounds of 32 mark words.
 __global__ void clear_marked_kernel(uint4* __restrict__ grad, int64_t total16, int unit_shift,
                                     uint32_t* __restrict__ marks, int64_t words) {
-  const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int slots = 32 << unit_shift;  // 16-byte slots under one word
-  for (int64_t base = warp * 32; base < words; base += warps * 32) {
-    const int64_t w = base + lane;
-    const uint32_t mine = w < words ? marks[w] : 0u;
-    if (mine != 0u) marks[w] = 0u;
-    uint32_t pending = __ballot_sync(0xffffffffu, mine != 0u);
-    while (pending != 0u) {
-      const int src = __ffs(pending) - 1;
-      pending &= pending - 1u;
-      const uint32_t m = __shfl_sync(0xffffffffu, mine, src);
-      const int64_t first = (base + src) * (int64_t)slots;
-      for (int s = lane; s < slots; s += 32) {
-        const int64_t at = first + s;
-        if (((m >> (s >> unit_shift)) & 1u) && at < total16) grad[at] = make_uint4(0u, 0u, 0u, 0u);
-      }
-    }
-  }
+  clear_marked_warp(grad, total16, unit_shift, marks, words, warp, warps, threadIdx.x & 31);
 }
 
 }  // namespace

@@ -228,6 +228,36 @@ struct LossSum<float> {
   }
 };
 
+// Zeroing of the marked units of a gradient buffer, by one warp of `warps` (this one is
+// `warp`): bit b of mark word w marks the 4-cell unit 32 w + b, i.e. the 16-byte slots
+// (32 w + b) << unit_shift onwards (unit_shift: log2 of the slots per unit, 2 for fp32
+// cells, 3 for fp64). The warp takes 32 consecutive words per round (one coalesced load,
+// one word per lane) and clears them; then, for every word that had marks, it zeroes the
+// word's slots as consecutive 16-byte stores (512 B per warp store), lanes of unmarked
+// units skipping theirs, so the stores stay coalesced however the marks are spread.
+__device__ __forceinline__ void clear_marked_warp(uint4* __restrict__ grad, int64_t total16,
+                                                  int unit_shift, uint32_t* __restrict__ marks,
+                                                  int64_t words, int64_t warp, int64_t warps,
+                                                  int lane) {
+  const int slots = 32 << unit_shift;  // 16-byte slots under one word
+  for (int64_t base = warp * 32; base < words; base += warps * 32) {
+    const int64_t w = base + lane;
+    const uint32_t mine = w < words ? marks[w] : 0u;
+    if (mine != 0u) marks[w] = 0u;
+    uint32_t pending = __ballot_sync(kFull, mine != 0u);
+    while (pending != 0u) {
+      const int src = __ffs(pending) - 1;
+      pending &= pending - 1u;
+      const uint32_t m = __shfl_sync(kFull, mine, src);
+      const int64_t first = (base + src) * (int64_t)slots;
+      for (int s = lane; s < slots; s += 32) {
+        const int64_t at = first + s;
+        if (((m >> (s >> unit_shift)) & 1u) && at < total16) grad[at] = make_uint4(0u, 0u, 0u, 0u);
+      }
+    }
+  }
+}
+
 template <typename Real>
 __device__ __forceinline__ LossSum<Real> warp_sum(LossSum<Real> x) {
 #pragma unroll
