@@ -94,10 +94,10 @@ typedef struct {
                                explicit rays pass their share's offset, and every ray is
                                sampled as in the unsplit batch */
   uint32_t* grad_marks;     /* optional device bitmap (NULL: none) of the gradient's 4-cell
-                               units: the backward and training entry points set bit
-                               (c/4) % 32 of word c/128 for every gradient cell c they write,
-                               so pgb_clear_marked can re-zero just those units. No
-                               counterpart in the reference. */
+                               units, pgb_mark_words(cells) words: the backward and training
+                               entry points set bit (c/4) % 32 of word c/128 for every
+                               gradient cell c they write, so pgb_clear_marked can re-zero
+                               just those units. No counterpart in the reference. */
 } pgb_rays;
 
 /* ---- fused render path (scripts/train.py:142-156 composed with src/ray_sampling.py,
@@ -394,9 +394,11 @@ int pgb_remove_noise(float* cells, const int32_t dims[3], int32_t kernel_size, d
 /* Zero `bytes` bytes at ptr (16-byte aligned) with a vectorised store kernel: the
  * gradient zeroing of optimizer.zero_grad() (scripts/train.py:180) and of a fresh .grad. */
 int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream);
+/* Words of the gradient mark bitmap (pgb_rays.grad_marks) of num_cells cells. */
+int64_t pgb_mark_words(int64_t num_cells);
 /* Zeroes the gradient units marked in grad_marks (pgb_rays.grad_marks: 4 cells per unit,
- * ceil(num_cells / 128) words) and clears the marks. A dense gradient buffer whose only
- * writes since it was last zero are marked steps is zero again afterwards: the zeroing of
+ * pgb_mark_words(num_cells) words) and clears the marks. A dense gradient buffer whose only writes since
+ * it was last zero are marked steps is zero again afterwards: the zeroing of
  * optimizer.zero_grad() (scripts/train.py:180) restricted to the cells a step wrote. cell
  * bytes: 16 (F32/BF16 grids' fp32 gradient) or 32 (F64). No counterpart in the reference. */
 int pgb_clear_marked(void* grad_cells, int32_t cell_bytes, int64_t num_cells, uint32_t* grad_marks,

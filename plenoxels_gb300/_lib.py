@@ -133,6 +133,7 @@ _SIGNATURES = {
     "pgb_composite_bwd": (c_int32, [_P, c_int32, c_int64, c_int32, _P, _P, _P]),
     "pgb_fill_zero": (c_int32, [_P, c_int64, _P]),
     "pgb_clear_marked": (c_int32, [_P, c_int32, c_int64, _P, _P]),
+    "pgb_mark_words": (c_int64, [c_int64]),
     "pgb_rgba_to_image": (c_int32, [_P, c_int32, _P, _P]),
     "pgb_splat_size": (c_int32, [POINTER(c_float), c_int32, POINTER(c_int32)]),
     "pgb_splat_preview": (c_int32, [_P, POINTER(c_int32), c_float, POINTER(c_float), c_float, c_int32, c_float,

@@ -381,6 +381,8 @@ int pgb_fill_zero(void* ptr, int64_t bytes, pgb_stream_t stream) {
   return op_fill_zero(ptr, bytes, stream);
 }
 
+int64_t pgb_mark_words(int64_t num_cells) { return num_cells > 0 ? mark_words(num_cells) : 0; }
+
 int pgb_clear_marked(void* grad_cells, int32_t cell_bytes, int64_t num_cells, uint32_t* grad_marks,
                      pgb_stream_t stream) {
   if (num_cells < 0 || (cell_bytes != 16 && cell_bytes != 32)) return PGB_ERR_ARG;

@@ -826,8 +826,9 @@ int op_rgba_to_image(const float* rgba, int res, uint8_t* out, cudaStream_t s) {
 }
 
 int op_clear_marked(void* grad, int cell_bytes, int64_t num_cells, uint32_t* marks, cudaStream_t s) {
-  const int64_t words = (num_cells + 127) / 128;
-  const int unit_shift = cell_bytes == 32 ? 3 : 2;  // log2 of 16-byte slots per 4-cell unit
+  const int64_t words = mark_words(num_cells);
+  // log2 of the 16-byte slots per unit: a cell is 1 (fp32 gradient) or 2 (fp64) slots
+  const int unit_shift = (cell_bytes == 32 ? 1 : 0) + kMarkCellsLog2;
   const int64_t total16 = num_cells * cell_bytes / 16;
   // one thread per word: each warp takes 32 consecutive words
   clear_marked_kernel<<<blocks_for(words), kThreads, 0, s>>>((uint4*)grad, total16, unit_shift,

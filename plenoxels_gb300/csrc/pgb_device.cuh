@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "plenoxels_gb300.h"
+#include "pgb_host.h"
 
 namespace pgb {
 
@@ -228,13 +229,16 @@ struct LossSum<float> {
   }
 };
 
+// Gradient marks (layout in pgb_host.h): the unit of a cell.
+__device__ __forceinline__ uint64_t mark_unit_of(uint64_t cell) { return cell >> kMarkCellsLog2; }
+
 // Zeroing of the marked units of a gradient buffer, by one warp of `warps` (this one is
-// `warp`): bit b of mark word w marks the 4-cell unit 32 w + b, i.e. the 16-byte slots
-// (32 w + b) << unit_shift onwards (unit_shift: log2 of the slots per unit, 2 for fp32
-// cells, 3 for fp64). The warp takes 32 consecutive words per round (one coalesced load,
-// one word per lane) and clears them; then, for every word that had marks, it zeroes the
-// word's slots as consecutive 16-byte stores (512 B per warp store), lanes of unmarked
-// units skipping theirs, so the stores stay coalesced however the marks are spread.
+// `warp`): bit b of mark word w marks unit 32 w + b, i.e. the 16-byte slots
+// (32 w + b) << unit_shift onwards (unit_shift: log2 of the 16-byte slots per unit). The
+// warp takes 32 consecutive words per round (one coalesced load, one word per lane) and
+// clears them; then, for every word that had marks, it zeroes the word's slots as
+// consecutive 16-byte stores (512 B per warp store), lanes of unmarked units skipping
+// theirs, so the stores stay coalesced however the marks are spread.
 __device__ __forceinline__ void clear_marked_warp(uint4* __restrict__ grad, int64_t total16,
                                                   int unit_shift, uint32_t* __restrict__ marks,
                                                   int64_t words, int64_t warp, int64_t warps,

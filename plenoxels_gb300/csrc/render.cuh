@@ -292,10 +292,10 @@ __device__ __forceinline__ void sample_value(const GridP<Real>& g, Real nx, Real
 #define PGB_SCATTER_ATTR __device__ __noinline__
 #endif
 
-// Marks the gradient unit of cell c (4 consecutive cells) in a bitmap of units: bit
-// (c / 4) % 32 of word c / 128.
+// Marks the gradient unit of cell c in the bitmap of units (mark_unit_of).
 __device__ __forceinline__ void mark_unit(uint32_t* marks, uint64_t c) {
-  atomicOr(marks + (c >> 7), 1u << ((uint32_t)(c >> 2) & 31u));
+  const uint64_t u = mark_unit_of(c);
+  atomicOr(marks + (u >> 5), 1u << ((uint32_t)u & 31u));
 }
 
 // Scatter dL/dvalue of one sample into the dense gradient (the autograd replay of the
@@ -348,8 +348,9 @@ PGB_SCATTER_ATTR void sample_scatter(const GridP<Real>& g, Real* grad, Real nx, 
         const uint64_t cell = (row + (uint64_t)iy) * (uint64_t)g.Z + (uint64_t)iz;
         grad_add(grad, cell, gv);
         if (marks != nullptr) {
-          const uint64_t word = cell >> 7;
-          const uint32_t bit = 1u << ((uint32_t)(cell >> 2) & 31u);
+          const uint64_t unit = mark_unit_of(cell);
+          const uint64_t word = unit >> 5;
+          const uint32_t bit = 1u << ((uint32_t)unit & 31u);
           if (mark_bits != 0u && word != mark_word) {
             atomicOr(marks + mark_word, mark_bits);
             mark_bits = 0u;

@@ -258,7 +258,7 @@ class FusedTrainStep:
         if zeroing not in ("fill", "marked"):
             raise ValueError(f"zeroing must be 'fill' or 'marked', got {zeroing!r}")
         cells = grid.numel() // 4
-        self._marks = ([torch.zeros((cells + 127) // 128, dtype=torch.int32, device=dev)
+        self._marks = ([torch.zeros(lib.pgb_mark_words(cells), dtype=torch.int32, device=dev)
                         for _ in self._grads] if zeroing == "marked" else None)
         self._cur = 0
         self._buf = 0  # index of the buffer the last launch wrote

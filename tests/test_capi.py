@@ -85,6 +85,8 @@ def test_status_strings_and_version(lib):
     assert lib.pgb_status_string(0) == b"ok"
     assert lib.pgb_status_string(-1) == b"invalid argument"
     assert lib.pgb_train_workspace_bytes() >= 8 * 8192
+    # one mark bit per 4-cell unit of the gradient
+    assert [lib.pgb_mark_words(n) for n in (0, 1, 128, 129, 256 ** 3)] == [0, 1, 1, 2, 256 ** 3 // 128]
 
 
 def test_argument_validation_without_launch(lib):

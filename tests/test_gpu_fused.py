@@ -418,14 +418,15 @@ def test_marked_zeroing_gives_the_dense_steps(mode, overlap):
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 @pytest.mark.parametrize("num_cells", [1000, 128 * 40 + 3, 256 * 1024 + 130])
 def test_clear_marked_zeroes_exactly_the_marked_units(dtype, num_cells):
-    """pgb_clear_marked zeroes the cells of every marked 4-cell unit (bit (c/4)%32 of word
-    c/128), leaves every other cell as it was, stops at num_cells (a ragged last unit and
-    word) and leaves the bitmap all zero; words with every bit set, none, and random
-    sparse bits."""
+    """pgb_clear_marked zeroes the cells of every marked unit (bit u%32 of word u/32, a
+    unit being the cells the library's mark layout groups, pgb_mark_words words), leaves
+    every other cell as it was, stops at num_cells (a ragged last unit and word) and
+    leaves the bitmap all zero; words with every bit set, none, and random sparse bits."""
     lib = _lib.load()
     rng = np.random.default_rng(num_cells)
-    words = (num_cells + 127) // 128
-    units = (num_cells + 3) // 4
+    words = lib.pgb_mark_words(num_cells)
+    per_unit = next(p for p in (1, 2, 4, 8) if ((num_cells + p - 1) // p + 31) // 32 == words)
+    units = (num_cells + per_unit - 1) // per_unit
     bits = rng.random(words * 32) < 0.05
     bits[: 32 * min(3, words)] = True  # full words at the start
     bits[32 * 5: 32 * 7] = False       # empty words
@@ -441,7 +442,7 @@ def test_clear_marked_zeroes_exactly_the_marked_units(dtype, num_cells):
                               torch.cuda.current_stream().cuda_stream)
     assert st == 0
     torch.cuda.synchronize()
-    cell_marked = torch.from_numpy(np.repeat(bits[:units], 4)[:num_cells]).to(DEV)
+    cell_marked = torch.from_numpy(np.repeat(bits[:units], per_unit)[:num_cells]).to(DEV)
     expect = torch.where(cell_marked[:, None], torch.zeros_like(before), before)
     assert torch.equal(grad, expect)
     assert int(marks.abs().sum()) == 0
