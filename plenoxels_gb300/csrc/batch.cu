@@ -68,6 +68,7 @@ struct BatchArgs {
   uint64_t seed;
   double loss_w;
   double inv_count;
+  float grad_scale;          // 2 * loss_w * inv_count, rounded on the host
   float* rgba_out;
   float* loss_out;
   unsigned long long* work;  // ray queue head
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
   const int lane = threadIdx.x & (kWarp - 1);
   const int wib = threadIdx.x >> 5;
   ChunkStage<float, K> cs(smem_raw + tab_bytes, wib);
-  const float grad_scale = (float)(2.0 * a.loss_w * a.inv_count);  // d(weighted MSE)/d pixel
+  const float grad_scale = a.grad_scale;  // d(weighted MSE)/d pixel
 
   for (;;) {
     unsigned long long rr = 0;
@@ -548,6 +549,7 @@ int pgb_batch_train(const pgb_scene* scenes, int32_t num_scenes, int32_t dtype, 
   a.seed = seed;
   a.loss_w = loss_weight;
   a.inv_count = num_rays > 0 ? 1.0 / (4.0 * (double)num_rays) : 0.0;
+  a.grad_scale = (float)(2.0 * a.loss_w * a.inv_count);
   a.rgba_out = rgba_out;
   a.loss_out = loss_out;
   a.work = reinterpret_cast<unsigned long long*>(workspace);

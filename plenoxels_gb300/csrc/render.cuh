@@ -82,6 +82,11 @@ struct RenderArgs {
   float beta_eps;
   double inv_samples;
   double* partials_beta;
+  // derived on the host (finish_args): GB300's fp64 rate is low, and every warp would
+  // otherwise evaluate these double expressions at its start
+  int use_beta;       // beta_w != 0
+  Real grad_scale;    // 2 * loss_w * inv_count: d(weighted MSE)/d pixel
+  Real beta_scale;    // beta_w * inv_samples * (1 + 2 eps)
 };
 
 template <typename Real>
@@ -134,7 +139,12 @@ __device__ __forceinline__ void load_ray(const RenderArgs<Real>& a, int64_t r, R
                                          bool need_target) {
   if (a.use_cameras) {
     // cameras get contiguous runs of rays (camera-major, src/ray_sampling.py:243)
-    const int c = (int)((r * (int64_t)a.C) / a.R);
+    // floor(r * C / R), in 32-bit arithmetic when r * C fits (the 64-bit divide is a long
+    // instruction sequence)
+    const uint64_t rc = (uint64_t)r * (uint64_t)a.C;
+    const int c = (rc >> 32) == 0 && ((uint64_t)a.R >> 32) == 0
+                      ? (int)((uint32_t)rc / (uint32_t)a.R)
+                      : (int)(rc / (uint64_t)a.R);
     const float* T = a.transforms + 16 * (int64_t)c;
     const uint64_t h = hash_stream(a.cam_seed, (uint64_t)r);
     const float u = hash_to_unit(h, 0u), v = hash_to_unit(h, 1u);
@@ -649,7 +659,7 @@ render_kernel(const RenderArgs<Real> a) {
   ChunkStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
   LossSum<Real> loss_lane;  // lane 0: squared errors of the warp's rays
   LossSum<Real> beta_lane;  // per lane: beta terms of its samples
-  const bool with_beta = PHASE == kTrain && a.beta_w != 0.0;
+  const bool with_beta = PHASE == kTrain && a.use_beta;
   // Exact early stop. With alpha clamped to [0,1], T is exactly 0 only behind an opaque
   // sample z (alpha_z = 1) or after an underflow, and every later sample then has weight
   // 0 and colour and alpha gradients 0. One term still reads them: z's own alpha gradient
@@ -661,8 +671,8 @@ render_kernel(const RenderArgs<Real> a) {
   const bool stop_at_zero = a.g.clip && !with_beta;
   constexpr uint32_t kAlphaBits = MODE == PGB_NEAREST ? 0x8u : 0x88888888u;
   // beta_w / (R*S) * (1 + 2 eps): the numerator of 1/(alpha+eps) + 1/(1-alpha+eps)
-  const Real beta_scale = (Real)(a.beta_w * a.inv_samples * (1.0 + 2.0 * (double)a.beta_eps));
-  const Real grad_scale = (Real)(2.0 * a.loss_w * a.inv_count);  // d(weighted MSE)/d pixel
+  const Real beta_scale = a.beta_scale;
+  const Real grad_scale = a.grad_scale;
   __shared__ double s_part[32];  // per-warp loss partials (training phase)
   __shared__ double s_part_beta[32];
   __shared__ unsigned s_done;    // warps of this block that finished (training phase)

@@ -89,6 +89,16 @@ RenderArgs<Real> render_args(const pgb_grid* g, const pgb_rays* r) {
   return a;
 }
 
+// The kernel arguments derived from the loss weights, in double on the host and rounded
+// to Real once, as the kernel would round them.
+template <typename Real>
+void finish_args(RenderArgs<Real>& a) {
+  a.use_beta = a.beta_w != 0.0 ? 1 : 0;
+  a.grad_scale = (Real)(2.0 * a.loss_w * a.inv_count);
+  // beta_w / (R*S) * (1 + 2 eps): the numerator of 1/(alpha+eps) + 1/(1-alpha+eps)
+  a.beta_scale = (Real)(a.beta_w * a.inv_samples * (1.0 + 2.0 * (double)a.beta_eps));
+}
+
 template <typename Real>
 int dispatch_render(const pgb_grid* g, const pgb_rays* r, RenderArgs<Real>& a, int phase,
                     cudaStream_t s);
@@ -96,6 +106,7 @@ int dispatch_render(const pgb_grid* g, const pgb_rays* r, RenderArgs<Real>& a, i
 template <>
 inline int dispatch_render<float>(const pgb_grid* g, const pgb_rays* r, RenderArgs<float>& a, int phase,
                            cudaStream_t s) {
+  finish_args(a);
   if (r->log_transmittance)
     return g->dtype == PGB_BF16 ? launch_render_logt_bf16(a, g->mode, phase, s)
                                 : launch_render_logt_f32(a, g->mode, phase, s);
@@ -105,6 +116,7 @@ inline int dispatch_render<float>(const pgb_grid* g, const pgb_rays* r, RenderAr
 template <>
 inline int dispatch_render<double>(const pgb_grid* g, const pgb_rays* r, RenderArgs<double>& a, int phase,
                             cudaStream_t s) {
+  finish_args(a);
   (void)r;  // check_rays rejects the log-sum form for fp64 grids
   return launch_render_f64(a, g->mode, phase, s);
 }
