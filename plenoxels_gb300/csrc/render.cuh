@@ -466,11 +466,13 @@ constexpr int kRenderMinThreads = kRenderThreads < kRenderThreadsK1 ? kRenderThr
 // their clamped values and clamp-pass bits, so the reverse pass reads the M - 1 chunks
 // before the last from here instead of gathering them from the grid again. Layout
 // [slot][field][K][32]: each lane reads back only what it wrote, without bank conflicts.
-template <typename Real, int K>
+template <typename Real, int K, int MSLOTS = (K == 1 ? PGB_STAGE_CHUNKS : 1), bool COORDS = true>
 struct ChunkStage {
-  static constexpr int M = K == 1 ? PGB_STAGE_CHUNKS : 1;
+  static constexpr int M = MSLOTS;
+  static constexpr bool kHasCoords = COORDS;
   static_assert((M & (M - 1)) == 0, "stage slots must be a power of two");
-  static constexpr int kCoordBytes = 3 * K * kWarp * (int)sizeof(Real);
+  static_assert(COORDS || M > 1, "a stage without coordinates holds values");
+  static constexpr int kCoordBytes = COORDS ? 3 * K * kWarp * (int)sizeof(Real) : 0;
   static constexpr int kValBytes = M > 1 ? 4 * K * kWarp * (int)sizeof(Real) + K * kWarp * 4 : 0;
   static constexpr int kSlotBytes = kCoordBytes + kValBytes;
   static constexpr int kBytesPerWarp = M * kSlotBytes;
@@ -481,6 +483,7 @@ struct ChunkStage {
   // chunk c is still in the stage when the reverse pass reaches it (last = last chunk)
   __device__ __forceinline__ static bool holds(int c, int last) { return M > 1 && c > last - M; }
   __device__ __forceinline__ void put(int c, int k, int lane, Real x, Real y, Real z) {
+    if constexpr (!COORDS) return;
     Real* n = reinterpret_cast<Real*>(slot(c));
     n[(0 * K + k) * kWarp + lane] = x;
     n[(1 * K + k) * kWarp + lane] = y;
@@ -529,10 +532,9 @@ PGB_RENDER_GATHER_ATTR void render_sample(const RenderArgs<Real>& a, const Ray<R
 
 // Gathers chunk `c` (K slots) of a ray into registers (and its coordinates into the
 // stage when the adjoint follows).
-template <typename Real, typename Store, int MODE, int K, bool ADJ>
+template <typename Real, typename Store, int MODE, int K, bool ADJ, typename Stage>
 __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ray<Real>& ray, int c,
-                                             int lane, Real v[K][4], uint32_t bits[K],
-                                             ChunkStage<Real, K>& cs) {
+                                             int lane, Real v[K][4], uint32_t bits[K], Stage& cs) {
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     const int s = (c * K + k) * kWarp + lane;
@@ -627,9 +629,25 @@ __device__ __forceinline__ Real pick4(const Real v[4], int i) {
   return i == 0 ? v[0] : (i == 1 ? v[1] : (i == 2 ? v[2] : v[3]));
 }
 
+// The render kernel's stage at 32-sample chunks: the values and clamp bits of the last
+// PGB_RENDER_STAGE_CHUNKS chunks, without their coordinates (the reverse pass recomputes
+// a sample's coordinates from its ray: cheaper than gathering a chunk from the grid
+// again). 256^3, 8192 rays x 256 samples: 8 chunks without coordinates (5 KB per warp)
+// 0.0928 ms per step; 4 chunks with them (4 KB) 0.1000 ms, without 0.0976 ms; 8 chunks
+// with them (8 KB, 192 KB of shared memory per SM, leaving little L1) 0.175 ms.
+#ifndef PGB_RENDER_STAGE_CHUNKS
+#define PGB_RENDER_STAGE_CHUNKS 8
+#endif
+#ifndef PGB_RENDER_STAGE_COORDS
+#define PGB_RENDER_STAGE_COORDS 0
+#endif
+template <typename Real, int K>
+using RenderStage = ChunkStage<Real, K, (K == 1 ? PGB_RENDER_STAGE_CHUNKS : 1),
+                               (K != 1 || PGB_RENDER_STAGE_COORDS != 0)>;
+
 template <typename Real, int K>
 constexpr int render_smem_bytes(int warps_per_block) {
-  return ChunkStage<Real, K>::kBytesPerWarp * warps_per_block;
+  return RenderStage<Real, K>::kBytesPerWarp * warps_per_block;
 }
 
 template <int MODE, int K>
@@ -656,7 +674,7 @@ render_kernel(const RenderArgs<Real> a) {
   const int64_t gw = (int64_t)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int64_t nw = (int64_t)gridDim.x * warps_per_block;
   const int nchunks = (a.S + kWarp * K - 1) / (kWarp * K);
-  ChunkStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
+  RenderStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
   LossSum<Real> loss_lane;  // lane 0: squared errors of the warp's rays
   LossSum<Real> beta_lane;  // per lane: beta terms of its samples
   const bool with_beta = PHASE == kTrain && a.use_beta;
@@ -785,7 +803,7 @@ render_kernel(const RenderArgs<Real> a) {
     for (int c = last; c >= 0; --c) {
       if (c != last) {
         __syncwarp();
-        if (ChunkStage<Real, K>::holds(c, last)) {  // the chunk's values are still staged
+        if (RenderStage<Real, K>::holds(c, last)) {  // the chunk's values are still staged
 #pragma unroll
           for (int k = 0; k < K; ++k) cs.get_vals(c, k, lane, v[k], bits[k]);
         } else {
@@ -840,7 +858,10 @@ render_kernel(const RenderArgs<Real> a) {
               !(dv[0] != Real(0) || dv[1] != Real(0) || dv[2] != Real(0) || dv[3] != Real(0)))
             continue;
           Real nx, ny, nz;
-          cs.get(c, k, lane, nx, ny, nz);
+          if constexpr (RenderStage<Real, K>::kHasCoords)
+            cs.get(c, k, lane, nx, ny, nz);
+          else
+            sample_coords(a, ray, (c * K + k) * kWarp + lane, nx, ny, nz);
           sample_scatter<Real, MODE>(a.g, a.grad, nx, ny, nz, dv, bk, a.grad_marks);
         }
       }
