@@ -142,6 +142,19 @@ PGB_BATCH_GATHER_ATTR bool batch_sample(const RenderArgs<float>& ra, const Ray<f
   return true;
 }
 
+// The batched kernel's stage at 32-sample chunks: the values and clamp bits of the last
+// PGB_BATCH_STAGE_CHUNKS chunks, with the coordinates recomputed from the ray in the
+// reverse pass when PGB_BATCH_STAGE_COORDS is 0 (as the single-scene kernel does).
+#ifndef PGB_BATCH_STAGE_CHUNKS
+#define PGB_BATCH_STAGE_CHUNKS 8
+#endif
+#ifndef PGB_BATCH_STAGE_COORDS
+#define PGB_BATCH_STAGE_COORDS 0
+#endif
+template <int K>
+using BatchStage = ChunkStage<float, K, (K == 1 ? PGB_BATCH_STAGE_CHUNKS : 1),
+                              (K != 1 || PGB_BATCH_STAGE_COORDS != 0)>;
+
 // MERGE: the trilinear scatter merges the warp's updates of the same cell
 // (warp_merged_scatter) before its atomics.
 template <typename Store, int MODE, int K, bool MERGE>
@@ -159,7 +172,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
   __syncthreads();
   const int lane = threadIdx.x & (kWarp - 1);
   const int wib = threadIdx.x >> 5;
-  ChunkStage<float, K> cs(smem_raw + tab_bytes, wib);
+  BatchStage<K> cs(smem_raw + tab_bytes, wib);
   const float grad_scale = a.grad_scale;  // d(weighted MSE)/d pixel
 
   for (;;) {
@@ -272,7 +285,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
     for (int c = last; c >= 0; --c) {
       if (c != last) {
         __syncwarp();
-        if (ChunkStage<float, K>::holds(c, last)) {  // the chunk's values are still staged
+        if (BatchStage<K>::holds(c, last)) {  // the chunk's values are still staged
 #pragma unroll
           for (int k = 0; k < K; ++k) cs.get_vals(c, k, lane, v[k], bits[k]);
         } else {
@@ -316,7 +329,12 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
             dv[0] = gpx[0] * w; dv[1] = gpx[1] * w; dv[2] = gpx[2] * w;
             dv[3] = tk * (G - S_after);
             has = dv[0] != 0.f || dv[1] != 0.f || dv[2] != 0.f || dv[3] != 0.f;
-            if (has) cs.get(c, k, lane, nx, ny, nz);
+            if (has) {
+              if constexpr (BatchStage<K>::kHasCoords)
+                cs.get(c, k, lane, nx, ny, nz);
+              else
+                sample_coords(ra, ray, (c * K + k) * kWarp + lane, nx, ny, nz);
+            }
           }
           warp_merged_scatter<float>(ra.g, grad, has, nx, ny, nz, dv, bk, lane);
         } else if (bk != 0u) {
@@ -324,7 +342,10 @@ __global__ void __launch_bounds__(kBatchMaxThreads, K == 1 ? PGB_BATCH_MIN_BLOCK
           float dv[4] = {gpx[0] * w, gpx[1] * w, gpx[2] * w, tk * (G - S_after)};
           if (!(dv[0] != 0.f || dv[1] != 0.f || dv[2] != 0.f || dv[3] != 0.f)) continue;
           float nx, ny, nz;
-          cs.get(c, k, lane, nx, ny, nz);
+          if constexpr (BatchStage<K>::kHasCoords)
+            cs.get(c, k, lane, nx, ny, nz);
+          else
+            sample_coords(ra, ray, (c * K + k) * kWarp + lane, nx, ny, nz);
           sample_scatter<float, MODE>(ra.g, grad, nx, ny, nz, dv, bk);
         }
       }
@@ -468,7 +489,7 @@ template <typename Store, int MODE, int K, bool MERGE>
 int launch_batch_k(const BatchArgs& a, int threads, cudaStream_t s) {
   const int warps = threads / kWarp;
   const size_t tab = (((size_t)a.num_scenes * sizeof(pgb_scene)) + 15) & ~(size_t)15;
-  const size_t smem = tab + (size_t)ChunkStage<float, K>::kBytesPerWarp * warps;
+  const size_t smem = tab + (size_t)BatchStage<K>::kBytesPerWarp * warps;
   auto kern = batch_train_kernel<Store, MODE, K, MERGE>;
   int dev = 0;
   cudaGetDevice(&dev);
