@@ -466,14 +466,20 @@ constexpr int kRenderMinThreads = kRenderThreads < kRenderThreadsK1 ? kRenderThr
 // their clamped values and clamp-pass bits, so the reverse pass reads the M - 1 chunks
 // before the last from here instead of gathering them from the grid again. Layout
 // [slot][field][K][32]: each lane reads back only what it wrote, without bank conflicts.
-template <typename Real, int K, int MSLOTS = (K == 1 ? PGB_STAGE_CHUNKS : 1), bool COORDS = true>
+template <typename Real, int K, int MSLOTS = (K == 1 ? PGB_STAGE_CHUNKS : 1), bool COORDS = true,
+          bool TS = false>
 struct ChunkStage {
   static constexpr int M = MSLOTS;
   static constexpr bool kHasCoords = COORDS;
+  static constexpr bool kHasTs = TS;  // the transmittance of every sample too
   static_assert((M & (M - 1)) == 0, "stage slots must be a power of two");
   static_assert(COORDS || M > 1, "a stage without coordinates holds values");
+  static_assert(!TS || M > 1, "transmittances are held with the values");
   static constexpr int kCoordBytes = COORDS ? 3 * K * kWarp * (int)sizeof(Real) : 0;
-  static constexpr int kValBytes = M > 1 ? 4 * K * kWarp * (int)sizeof(Real) + K * kWarp * 4 : 0;
+  static constexpr int kVBytes = 4 * K * kWarp * (int)sizeof(Real);
+  static constexpr int kBitsBytes = K * kWarp * 4;
+  static constexpr int kTsBytes = TS ? K * kWarp * (int)sizeof(Real) : 0;
+  static constexpr int kValBytes = M > 1 ? kVBytes + kBitsBytes + kTsBytes : 0;
   static constexpr int kSlotBytes = kCoordBytes + kValBytes;
   static constexpr int kBytesPerWarp = M * kSlotBytes;
   unsigned char* base;
@@ -500,7 +506,7 @@ struct ChunkStage {
       Real* w = reinterpret_cast<Real*>(slot(c) + kCoordBytes);
 #pragma unroll
       for (int ch = 0; ch < 4; ++ch) w[(ch * K + k) * kWarp + lane] = v[ch];
-      reinterpret_cast<uint32_t*>(slot(c) + kCoordBytes + 4 * K * kWarp * sizeof(Real))[k * kWarp + lane] = bits;
+      reinterpret_cast<uint32_t*>(slot(c) + kCoordBytes + kVBytes)[k * kWarp + lane] = bits;
     }
   }
   __device__ __forceinline__ void get_vals(int c, int k, int lane, Real v[4], uint32_t& bits) const {
@@ -508,8 +514,16 @@ struct ChunkStage {
       const Real* w = reinterpret_cast<const Real*>(slot(c) + kCoordBytes);
 #pragma unroll
       for (int ch = 0; ch < 4; ++ch) v[ch] = w[(ch * K + k) * kWarp + lane];
-      bits = reinterpret_cast<const uint32_t*>(slot(c) + kCoordBytes + 4 * K * kWarp * sizeof(Real))[k * kWarp + lane];
+      bits = reinterpret_cast<const uint32_t*>(slot(c) + kCoordBytes + kVBytes)[k * kWarp + lane];
     }
+  }
+  __device__ __forceinline__ void put_t(int c, int k, int lane, Real t) {
+    if constexpr (TS) reinterpret_cast<Real*>(slot(c) + kCoordBytes + kVBytes + kBitsBytes)[k * kWarp + lane] = t;
+  }
+  __device__ __forceinline__ Real get_t(int c, int k, int lane) const {
+    if constexpr (TS)
+      return reinterpret_cast<const Real*>(slot(c) + kCoordBytes + kVBytes + kBitsBytes)[k * kWarp + lane];
+    return Real(0);
   }
 };
 
@@ -641,13 +655,22 @@ __device__ __forceinline__ Real pick4(const Real v[4], int i) {
 #ifndef PGB_RENDER_STAGE_COORDS
 #define PGB_RENDER_STAGE_COORDS 0
 #endif
-template <typename Real, int K>
-using RenderStage = ChunkStage<Real, K, (K == 1 ? PGB_RENDER_STAGE_CHUNKS : 1),
-                               (K != 1 || PGB_RENDER_STAGE_COORDS != 0)>;
+// The staged chunks' transmittances as well (0: never, 1: always, 2: for the log-sum
+// transmittance only). Recomputing them in the reverse pass is a warp scan; for the
+// compensated log-sum it is a costly one. 512^3 log-sum, 65,536 rays x 512: 0.4567 ms
+// staged against 0.4865 ms; 256^3 product: 0.0965 against 0.0934 ms.
+#ifndef PGB_RENDER_STAGE_TS
+#define PGB_RENDER_STAGE_TS 2
+#endif
+template <typename Real, int K, bool LOGT = false>
+using RenderStage =
+    ChunkStage<Real, K, (K == 1 ? PGB_RENDER_STAGE_CHUNKS : 1),
+               (K != 1 || PGB_RENDER_STAGE_COORDS != 0),
+               (K == 1 && (PGB_RENDER_STAGE_TS == 1 || (PGB_RENDER_STAGE_TS == 2 && LOGT)))>;
 
-template <typename Real, int K>
+template <typename Real, int K, bool LOGT = false>
 constexpr int render_smem_bytes(int warps_per_block) {
-  return RenderStage<Real, K>::kBytesPerWarp * warps_per_block;
+  return RenderStage<Real, K, LOGT>::kBytesPerWarp * warps_per_block;
 }
 
 template <int MODE, int K>
@@ -674,7 +697,7 @@ render_kernel(const RenderArgs<Real> a) {
   const int64_t gw = (int64_t)blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int64_t nw = (int64_t)gridDim.x * warps_per_block;
   const int nchunks = (a.S + kWarp * K - 1) / (kWarp * K);
-  RenderStage<Real, K> cs(smem_raw, threadIdx.x >> 5);
+  RenderStage<Real, K, LOGT> cs(smem_raw, threadIdx.x >> 5);
   LossSum<Real> loss_lane;  // lane 0: squared errors of the warp's rays
   LossSum<Real> beta_lane;  // per lane: beta terms of its samples
   const bool with_beta = PHASE == kTrain && a.use_beta;
@@ -730,6 +753,10 @@ render_kernel(const RenderArgs<Real> a) {
         T = isinf(LT) ? Real(0) : (Real)expf(LT + LC);
       } else {
         T = scan_chunk<Real, K>(v, T, lane, Ts);
+      }
+      if (ADJ) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) cs.put_t(c, k, lane, Ts[k]);
       }
 #pragma unroll
       for (int k = 0; k < K; ++k) {
@@ -803,13 +830,17 @@ render_kernel(const RenderArgs<Real> a) {
     for (int c = last; c >= 0; --c) {
       if (c != last) {
         __syncwarp();
-        if (RenderStage<Real, K>::holds(c, last)) {  // the chunk's values are still staged
+        const bool staged = RenderStage<Real, K, LOGT>::holds(c, last);
+        if (staged) {  // the chunk's values are still staged
 #pragma unroll
           for (int k = 0; k < K; ++k) cs.get_vals(c, k, lane, v[k], bits[k]);
         } else {
           gather_chunk<Real, Store, MODE, K, true>(a, ray, c, lane, v, bits, cs);
         }
-        if constexpr (LOGT) {
+        if (RenderStage<Real, K, LOGT>::kHasTs && staged) {  // the forward pass's transmittances
+#pragma unroll
+          for (int k = 0; k < K; ++k) Ts[k] = cs.get_t(c, k, lane);
+        } else if constexpr (LOGT) {
           float l = __shfl_sync(kFull, LTstart, c), lc = __shfl_sync(kFull, LCstart, c);
           scan_chunk_log<K>(v, l, lc, lane, Ts);
         } else {
@@ -858,7 +889,7 @@ render_kernel(const RenderArgs<Real> a) {
               !(dv[0] != Real(0) || dv[1] != Real(0) || dv[2] != Real(0) || dv[3] != Real(0)))
             continue;
           Real nx, ny, nz;
-          if constexpr (RenderStage<Real, K>::kHasCoords)
+          if constexpr (RenderStage<Real, K, LOGT>::kHasCoords)
             cs.get(c, k, lane, nx, ny, nz);
           else
             sample_coords(a, ray, (c * K + k) * kWarp + lane, nx, ny, nz);

@@ -15,7 +15,7 @@ template <typename Real, typename Store, int MODE, int K, int PHASE, bool LOGT>
 int launch_render_k(const RenderArgs<Real>& a, cudaStream_t s) {
   constexpr int kThreads = render_threads<MODE, K>();
   constexpr int kWarpsPerBlock = kThreads / kWarp;
-  constexpr int kSmem = render_smem_bytes<Real, K>(kWarpsPerBlock);
+  constexpr int kSmem = render_smem_bytes<Real, K, LOGT>(kWarpsPerBlock);
   // the dynamic shared-memory opt-in (dynamic + static may pass 48 KiB) is per device:
   // set it on first use of each device
   static int configured[64] = {0};
