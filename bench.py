@@ -52,7 +52,7 @@ PRECISION = dict(workload="precision form, 512^3 grid (64 blobs, uniform RGB), 2
                  cameras=200, image=800, rays=65536, samples=512, mode="trilinear", near=2.0,
                  far=6.0, blobs=64, rgb="uniform", camera_angle_x=0.691, grid_seed=21,
                  camera_seed=22, ground_truth_seed=23)
-NCU_TRAFFIC_BYTES = 148_040_704 + 14_042_624  # DRAM read + write, one launch
+NCU_TRAFFIC_BYTES = 145_588_480 + 12_452_096  # DRAM read + write, one launch
 METRIC = "train rays/sec (fwd+bwd)"
 # samples per chunk of the fused step (0: the library's choice)
 CHUNK = 0
