@@ -455,19 +455,18 @@ constexpr int kRenderThreadsK1 = PGB_RENDER_THREADS_K1;
 constexpr int kRenderMinThreads = kRenderThreads < kRenderThreadsK1 ? kRenderThreads
                                                                      : kRenderThreadsK1;
 
-// Chunks of 32 samples whose values the render kernel keeps per warp for its reverse pass.
-#ifndef PGB_STAGE_CHUNKS
-#define PGB_STAGE_CHUNKS 4
-#endif
 
-// The per-warp shared-memory stage of the render and batched kernels. It holds the normalised coordinates of
-// the last M chunks, so the reverse pass does not recompute the stratification hash and
-// the exact divisions. With 32-sample chunks (K = 1, M = PGB_STAGE_CHUNKS) it also holds
-// their clamped values and clamp-pass bits, so the reverse pass reads the M - 1 chunks
-// before the last from here instead of gathering them from the grid again. Layout
-// [slot][field][K][32]: each lane reads back only what it wrote, without bank conflicts.
-template <typename Real, int K, int MSLOTS = (K == 1 ? PGB_STAGE_CHUNKS : 1), bool COORDS = true,
-          bool TS = false>
+// The per-warp shared-memory stage of the render and batched kernels: per chunk slot,
+// for the last M chunks,
+//   - the normalised coordinates (COORDS; otherwise the reverse pass recomputes them from
+//     the ray: the stratification hash and the exact divisions),
+//   - with M > 1, the clamped values and clamp-pass bits, so the reverse pass reads the
+//     M - 1 chunks before the last from here instead of gathering them from the grid
+//     again,
+//   - with TS, the forward pass's transmittances, so the reverse pass skips their scan.
+// Layout [slot][field][K][32]: each lane reads back only what it wrote, without bank
+// conflicts.
+template <typename Real, int K, int MSLOTS, bool COORDS = true, bool TS = false>
 struct ChunkStage {
   static constexpr int M = MSLOTS;
   static constexpr bool kHasCoords = COORDS;
