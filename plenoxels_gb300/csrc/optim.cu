@@ -41,7 +41,9 @@ __global__ void __launch_bounds__(kTvThreads) tv_sumsq_kernel(const float4* __re
   const int64_t YZ = (int64_t)Y * Z;
   const int XL = (X + gridDim.z - 1) / gridDim.z;
   const int x0 = blockIdx.z * XL, x1 = min(X, x0 + XL);
-  double acc_d = 0.0;
+  // fp32 runs of at most 32 cells folded into a TwoSum pair; the block and the grid then
+  // sum pairs (GB300's fp64 rate is low: fp64 sums made this pass fp64-bound)
+  LossSum<float> acc_s;
   if (z < Z && x0 < x1) {
     float acc = 0.f;
     int64_t i = (int64_t)x0 * YZ + (int64_t)y * Z + z;
@@ -55,52 +57,62 @@ __global__ void __launch_bounds__(kTvThreads) tv_sumsq_kernel(const float4* __re
         acc += sq4(c, nx);
       }
       c = nx;
-      if (((x - x0) & 31) == 31) {  // bound the fp32 run, then fold into fp64
-        acc_d += acc;
+      if (((x - x0) & 31) == 31) {  // bound the fp32 run
+        acc_s.add(acc);
         acc = 0.f;
       }
     }
-    acc_d += acc;
+    acc_s.add(acc);
   }
-  __shared__ double red[kTvThreads];
+  // block: warps in warp order (kTvThreads / 32 warp partials), one pair per block
+  __shared__ double red[kTvThreads / 32];
   __shared__ bool last;
-  red[threadIdx.x] = acc_d;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  acc_s = warp_sum(acc_s);
+  if (lane == 0) acc_s.store(&red[wid]);
   __syncthreads();
-  for (int w = kTvThreads / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
   const unsigned nblocks = gridDim.x * gridDim.y * gridDim.z;
   const unsigned bid = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
   if (threadIdx.x == 0) {
-    partials[bid] = red[0];
+    LossSum<float> b;
+    for (int w = 0; w < kTvThreads / 32; ++w) b.add(LossSum<float>::load_volatile(&red[w]));
+    b.store(partials + bid);
     __threadfence();
     last = atomicAdd(counter, 1u) == nblocks - 1u;
   }
   __syncthreads();
   if (last) {
+    // the block pairs, thread-strided, then the warps in order
     __threadfence();
-    double s = 0.0;
-    for (unsigned b = threadIdx.x; b < nblocks; b += blockDim.x) s += ((volatile double*)partials)[b];
-    red[threadIdx.x] = s;
+    LossSum<float> t;
+    for (unsigned b = threadIdx.x; b < nblocks; b += blockDim.x) t.add(LossSum<float>::load_cg(partials + b));
+    t = warp_sum(t);
     __syncthreads();
-    for (int w = kTvThreads / 2; w > 0; w >>= 1) {
-      if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-      __syncthreads();
-    }
+    if (lane == 0) t.store(&red[wid]);
+    __syncthreads();
     if (threadIdx.x == 0) {
-      out[0] = red[0];
+      LossSum<float> total;
+      for (int w = 0; w < kTvThreads / 32; ++w) total.add(LossSum<float>::load_volatile(&red[w]));
+      out[0] = total.value();
       *counter = 0u;
     }
   }
 }
 
+// weight / sqrt(q) for the TV gradient, in fp32 arithmetic as the reference takes the TV
+// norm (torch.sqrt of an fp32 sum; scripts/train.py:62); 0 when q is not positive (a
+// constant grid: sqrt is not differentiable at 0). One conversion from the double sum and
+// no other fp64 work per thread.
+__device__ __forceinline__ float tv_scale(double q, float weight) {
+  const float qf = (float)q;
+  return qf > 0.f ? __fdiv_rn(weight, __fsqrt_rn(qf)) : 0.f;
+}
+
 __global__ void __launch_bounds__(kTvThreads) tv_grad_kernel(const float4* __restrict__ v, int X, int Y,
                                                              int Z, const double* __restrict__ sumsq,
                                                              float weight, float4* __restrict__ grad) {
-  const double q = sumsq[0];
-  if (!(q > 0.0)) return;  // a constant grid: sqrt is not differentiable at 0
-  const float c = (float)((double)weight / sqrt(q));
+  const float c = tv_scale(sumsq[0], weight);
+  if (c == 0.f) return;  // no TV weight, or a constant grid
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   const int XL = (X + gridDim.z - 1) / gridDim.z;
@@ -174,9 +186,8 @@ __global__ void __launch_bounds__(kTvThreads) adam_tv_kernel(
     const float4* __restrict__ pin, float4* __restrict__ pout, float4* __restrict__ g,
     float4* __restrict__ mo, float4* __restrict__ so, float4* __restrict__ acc, int X, int Y,
     int Z, const double* __restrict__ sumsq, float weight, AdamConst k, int zero_grad) {
-  const double q = sumsq[0];
-  const bool tv = q > 0.0;  // a constant grid: no TV term (as tv_grad_kernel)
-  const float c = tv ? (float)((double)weight / sqrt(q)) : 0.f;
+  const float c = tv_scale(sumsq[0], weight);
+  const bool tv = c != 0.f;  // no TV weight, or a constant grid (as tv_grad_kernel)
   const int z = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   const int XL = (X + gridDim.z - 1) / gridDim.z;
