@@ -645,7 +645,9 @@ def main():
     bufs = [torch.empty(10 * R, device=dev) for _ in range(2)]
     buf_views = [views(x) for x in bufs]
     copy_stream = torch.cuda.Stream(device=dev)
-    loss_host = torch.empty(args.steps + args.warmup, dtype=torch.float32).pin_memory()
+    # each step's losses land in its own row of a pinned host buffer: the kernel writes them
+    # there (the GPU addresses pinned host memory), so the read-back needs no copy call
+    loss_host = torch.zeros(args.steps + args.warmup + 1, 2, dtype=torch.float32).pin_memory()
     h2d = host[0].numel() * host[0].element_size()
     copied = [torch.cuda.Event(), torch.cuda.Event()]  # block b holds its batch
     free = [torch.cuda.Event(), torch.cuda.Event()]    # the step that last read block b has run
@@ -664,15 +666,16 @@ def main():
 
     def run(i, b):
         stream.wait_event(copied[b])
-        loss = step.step_rays(*buf_views[b])
+        step.step_rays(*buf_views[b], loss_out=loss_host[i])
         allreduce_gradient(step.grad)
-        loss_host[i].copy_(loss, non_blocking=True)
         free[b].record(stream)
         used[b] = True
 
     nxt = pipelined(0)
     for i in range(args.warmup):
-        cur, nxt = nxt, pipelined(i + 1)
+        cur = nxt
+        if i + 1 < args.warmup:
+            nxt = pipelined(i + 1)
         run(i, cur)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -685,6 +688,9 @@ def main():
         run(i, cur)
     e1.record(stream)
     torch.cuda.synchronize(dev)
+    read_back = loss_host[args.warmup:args.warmup + args.steps, 0]
+    assert bool(torch.isfinite(read_back).all()) and bool((read_back > 0).all()), \
+        "every timed step's loss must reach the host"
     e2e_ms = e0.elapsed_time(e1) / args.steps
     if world > 1:
         tt = torch.tensor([e2e_ms], device=dev)

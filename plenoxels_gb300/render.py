@@ -314,8 +314,24 @@ class FusedTrainStep:
         self._attach()
         return buf
 
-    def _launch(self, rdesc, target, rgba_out, zero_grad):
+    def _loss_target(self, loss_out):
+        """Where the step writes [weighted MSE, beta term]: self.losses, or loss_out, a
+        contiguous tensor of at least two elements of the step's dtype on this GPU or in
+        pinned host memory. Pinned host memory is addressable by the GPU under unified
+        addressing, so the kernel writes the loss there itself: the result reaches the
+        host without a separate copy."""
+        if loss_out is None:
+            return self.losses
+        if loss_out.dtype != self.real or loss_out.numel() < 2 or not loss_out.is_contiguous():
+            raise ValueError(f"loss_out must be a contiguous {self.real} tensor of >= 2 elements")
+        if not (loss_out.is_cuda and loss_out.device == self.grid.device) and not (
+                loss_out.device.type == "cpu" and loss_out.is_pinned()):
+            raise ValueError("loss_out must be on the grid's GPU or in pinned host memory")
+        return loss_out
+
+    def _launch(self, rdesc, target, rgba_out, zero_grad, loss_out=None):
         lib = _lib.load()
+        losses = self._loss_target(loss_out)
         grad = self._gradient_for_step(zero_grad)
         if self._marks is not None:
             rdesc.grad_marks = ptr(self._marks[self._buf])
@@ -327,22 +343,25 @@ class FusedTrainStep:
             ev[0].record(stream)
         if self.beta == 0.0:
             check(lib.pgb_render_train(gdesc, rdesc, ptr(target), self.loss_weight, ptr(rgba_out),
-                                       ptr(grad), ptr(self.losses), ptr(self.workspace),
+                                       ptr(grad), ptr(losses), ptr(self.workspace),
                                        stream.cuda_stream), "train step")
         else:
             terms = _lib.PgbLossTerms(self.loss_weight, self.beta, self.beta_eps)
             check(lib.pgb_render_train_terms(gdesc, rdesc, ptr(target), terms, ptr(rgba_out),
-                                             ptr(grad), ptr(self.losses), ptr(self.workspace),
+                                             ptr(grad), ptr(losses), ptr(self.workspace),
                                              stream.cuda_stream), "train step")
         if ev is not None:
             ev[1].record(stream)
             self.kernel_events.append(ev)
-        return self.loss
+        return self.loss if loss_out is None else loss_out[0]
 
-    def step_rays(self, origins, dirs, target, rgba_out=None, zero_grad=True, first_ray=0):
+    def step_rays(self, origins, dirs, target, rgba_out=None, zero_grad=True, first_ray=0,
+                  loss_out=None):
         """Explicit rays [R,3] and their target pixels [R,4]. first_ray: index of the first
         of these rays in the stratification stream, for ranks that each take a share of
-        one batch (distributed.shard_rays) and must sample it as the whole batch would."""
+        one batch (distributed.shard_rays) and must sample it as the whole batch would.
+        loss_out: where the losses go instead of self.losses (see _loss_target), e.g. a
+        pinned host buffer, so that reading a step's loss on the host needs no copy."""
         require_cuda(origins, dirs, target)
         _check_rays(self.grid, origins, dirs)
         if target.shape != (origins.shape[0], 4) or target.dtype != self.real:
@@ -350,10 +369,10 @@ class FusedTrainStep:
         rdesc = _rays_desc(origins, dirs, origins.shape[0], self.num_samples, self.delta_step,
                            self.stratified, self.seed, self.term_threshold, background=self.background,
                            log_t=self.log_t, chunk_samples=self.chunk_samples, first_ray=first_ray)
-        return self._launch(rdesc, target.contiguous(), rgba_out, zero_grad)
+        return self._launch(rdesc, target.contiguous(), rgba_out, zero_grad, loss_out)
 
     def step_cameras(self, transforms, images, camera_angle_x, num_rays, ray_seed, near=0.0,
-                     rgba_out=None, zero_grad=True):
+                     rgba_out=None, zero_grad=True, loss_out=None):
         """Rays generated in-kernel: num_rays spread camera-major over the cameras, pixel
         positions from the counter hash of ray_seed, origins moved `near` along each ray;
         targets are the sampled pixels of images [C,H,W,4]."""
@@ -362,4 +381,4 @@ class FusedTrainStep:
         rdesc = _rays_desc(None, None, num_rays, self.num_samples, self.delta_step, self.stratified,
                            self.seed, self.term_threshold, cameras=cams, background=self.background,
                            log_t=self.log_t, chunk_samples=self.chunk_samples)
-        return self._launch(rdesc, None, rgba_out, zero_grad)
+        return self._launch(rdesc, None, rgba_out, zero_grad, loss_out)

@@ -446,3 +446,29 @@ def test_clear_marked_zeroes_exactly_the_marked_units(dtype, num_cells):
     expect = torch.where(cell_marked[:, None], torch.zeros_like(before), before)
     assert torch.equal(grad, expect)
     assert int(marks.abs().sum()) == 0
+
+
+@pytest.mark.parametrize("mode", ["trilinear", "nearest"])
+def test_loss_written_into_pinned_host_memory(mode):
+    """loss_out in pinned host memory: the kernel writes the step's losses there directly,
+    the same values as into the step's own device buffer (same inputs, same kernel), and
+    the gradient is the same; other tensors are rejected."""
+    grid, T, imgs, o, d, target, delta = _scene(24, 3, 200, 61, S=96)
+    pd = scenes.points_distance(24)
+    g = grid.to(DEV)
+    od, dd, td = o.to(DEV), d.to(DEV), target.to(DEV)
+    a = pg.FusedTrainStep(g, pd, 96, delta, mode=mode, stratified=True, seed=4, beta=1e-3)
+    b = pg.FusedTrainStep(g, pd, 96, delta, mode=mode, stratified=True, seed=4, beta=1e-3)
+    host = torch.full((2,), -1.0, dtype=torch.float32).pin_memory()
+    la = a.step_rays(od, dd, td)
+    lb = b.step_rays(od, dd, td, loss_out=host)
+    torch.cuda.synchronize()
+    assert lb.data_ptr() == host.data_ptr()
+    assert float(host[0]) == float(la) and float(host[1]) == float(a.losses[1])
+    _grad_close(b.grad, a.grad, rel=1e-6)  # float atomics: run-dependent summation order
+    with pytest.raises(ValueError):
+        b.step_rays(od, dd, td, loss_out=torch.zeros(2))  # not pinned
+    with pytest.raises(ValueError):
+        b.step_rays(od, dd, td, loss_out=torch.zeros(2, dtype=torch.float64).pin_memory())
+    with pytest.raises(ValueError):
+        b.step_rays(od, dd, td, loss_out=torch.zeros(1).pin_memory())
