@@ -198,3 +198,18 @@ def test_long_rays_take_a_tile_that_covers_them():
     np.testing.assert_allclose(step.rgba.cpu().numpy(), rgba_ref.numpy(), rtol=1e-5, atol=2e-6)
     np.testing.assert_allclose(loss, loss_ref, rtol=1e-5)
     assert _grad_err(step, grads) < 1e-4
+
+
+def test_loss_over_many_rays_is_the_mean_squared_error_of_their_rgba():
+    """5760 rays: the ordered loss sum spans several blocks of its kernel; the step's loss
+    equals the mean over rays and channels of (rgba - target)^2 from its own outputs."""
+    problem = _make(torch.float32, seed=7)
+    for p in problem:
+        p["o"], p["d"], p["tgt"] = p["o"].repeat(6, 1), p["d"].repeat(6, 1), p["tgt"].repeat(6, 1)
+    step, R = _batch(problem, term_threshold=0.0)
+    assert R > 4 * 1024
+    loss = float(step.step())
+    torch.cuda.synchronize()
+    tgt = torch.cat([p["tgt"] for p in problem]).to(DEV).double()
+    ref = float(((step.rgba.double() - tgt) ** 2).mean())
+    np.testing.assert_allclose(loss, ref, rtol=1e-6)
