@@ -544,7 +544,7 @@ PGB_RENDER_GATHER_ATTR void render_sample(const RenderArgs<Real>& a, const Ray<R
 }
 
 // Gathers chunk `c` (K slots) of a ray into registers (and its coordinates into the
-// stage when the adjoint follows).
+// stage when the adjoint follows and the stage keeps coordinates).
 template <typename Real, typename Store, int MODE, int K, bool ADJ, typename Stage>
 __device__ __forceinline__ void gather_chunk(const RenderArgs<Real>& a, const Ray<Real>& ray, int c,
                                              int lane, Real v[K][4], uint32_t bits[K], Stage& cs) {
