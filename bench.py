@@ -58,8 +58,14 @@ METRIC = "train rays/sec (fwd+bwd)"
 CHUNK = 0
 # how a gradient buffer is re-zeroed for its next step: "marked" clears the 4-cell units
 # its previous step wrote (the step's kernel marks them); "fill" writes the whole buffer.
-# The bench reads no gradient and adds nothing into it, so both give the same steps.
+# On one GPU the bench reads no gradient and adds nothing into it, so both give the same
+# steps. Ranks of a multi-GPU run sum their gradients in place (all-reduce), which writes
+# cells no local step marked, so they fill.
 ZEROING = "marked"
+
+
+def zeroing_for(world):
+    return ZEROING if world == 1 else "fill"
 
 
 def _peaks():
@@ -573,7 +579,7 @@ def main():
     # weak scaling: R rays per rank, each rank's MSE weighted by its share of R * world
     step = pg.FusedTrainStep(grid, pd, S, delta, mode=W["mode"], stratified=True, seed=7,
                              loss_weight=1.0 / world, overlap_zero=True, chunk_samples=CHUNK,
-                             zeroing=ZEROING)
+                             zeroing=zeroing_for(world))
     stream = torch.cuda.current_stream(dev)
 
     def train(i):
@@ -737,7 +743,7 @@ def main():
             "data": "synthetic",
             "config": dict(W, l2="inputs larger than L2: 256 MiB grid read and 256 MiB gradient "
                                  "zeroed + scattered every step, 1 GiB of target images",
-                           chunk_samples=CHUNK, gradient_zeroing=ZEROING,
+                           chunk_samples=CHUNK, gradient_zeroing=zeroing_for(world),
                            parallelism=f"dp{world}" if world > 1 else "single"),
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "clocks": clk.summary()}

@@ -218,7 +218,8 @@ class FusedTrainStep:
     last step wrote (the kernel marks them in a bitmap of the buffer, pgb_clear_marked)
     instead of writing the whole buffer. Every step still starts from an all-zero dense
     gradient, provided the caller only reads the gradient buffers (an optimizer that
-    reads grid.grad, or zeroes it) and does not add into them.
+    reads grid.grad, or zeroes it) and does not add into them; an in-place all-reduce of
+    the gradient over ranks adds into them.
     """
 
     def __init__(self, grid, points_distance, num_samples, delta_step, mode="trilinear",
