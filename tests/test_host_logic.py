@@ -38,3 +38,16 @@ def test_batched_tiles_cover_the_longest_ray():
         stub = types.SimpleNamespace(max_samples=S)
         got = {k for k in (1, 2, 4, 8) if BatchedTrainStep._tile_fits(stub, (k, 256))}
         assert got == fits, (S, got)
+
+
+def test_bench_zeroes_multi_rank_gradients_densely():
+    """Marked zeroing clears only the cells a rank's own steps wrote; an in-place
+    all-reduce over ranks writes others, so multi-rank bench runs use the dense fill."""
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py")
+    spec = importlib.util.spec_from_file_location("bench_module", path)
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    assert bench.zeroing_for(1) == bench.ZEROING
+    assert all(bench.zeroing_for(n) == "fill" for n in (2, 4, 8))
