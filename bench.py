@@ -68,6 +68,28 @@ def zeroing_for(world):
     return ZEROING if world == 1 else "fill"
 
 
+# CUDA events bracket every KERNEL_EVENT_EVERY-th launch of the fused kernel in a timed
+# region. Events around every launch add ~3 us to each step (0.0925 against 0.0893 ms at
+# the headline workload) and, by leaving gaps in which the side-stream gradient clear runs
+# alone, understate the kernel's time inside a real step (0.089 against 0.093 ms).
+KERNEL_EVENT_EVERY = 4
+
+
+def timed_launches(step, steps, launch):
+    """Runs launch(i) for i < steps with the fused kernel's events on a sample of them;
+    returns the (start, end) event pairs."""
+    events = []
+    for i in range(steps):
+        step.kernel_events = events if i % KERNEL_EVENT_EVERY == 0 else None
+        launch(i)
+    step.kernel_events = None
+    return events
+
+
+def mean_kernel_ms(events):
+    return sum(a.elapsed_time(b) for a, b in events) / max(1, len(events))
+
+
 def _peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -266,15 +288,14 @@ def storage_leg(pg, grid, T, imgs, W, dev, dtype, steps, warmup, mode=None, zero
     for i in range(warmup):
         step.step_cameras(T, imgs, W["camera_angle_x"], R, 5000 + i, near=W["near"])
     torch.cuda.synchronize(dev)
-    step.kernel_events = []
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0.record(stream)
-    for i in range(steps):
-        step.step_cameras(T, imgs, W["camera_angle_x"], R, 6000 + i, near=W["near"])
+    events = timed_launches(step, steps, lambda i: step.step_cameras(
+        T, imgs, W["camera_angle_x"], R, 6000 + i, near=W["near"]))
     t1.record(stream)
     torch.cuda.synchronize(dev)
     ms = t0.elapsed_time(t1) / steps
-    kern = sum(a.elapsed_time(b) for a, b in step.kernel_events) / steps
+    kern = mean_kernel_ms(events)
     return {"value": R / (ms / 1e3), "unit": "rays/s", "ms_per_step": ms, "kernel_ms": kern,
             "storage": str(dtype).replace("torch.", ""), "note": "same workload, fp32 arithmetic "
             "and gradients, cells stored in this type"}
@@ -391,7 +412,8 @@ def batched_leg(pg, dev, steps=30, seed=11, num_scenes=64):
         per_cam = -(-n // 4)
         T = torch.from_numpy(scenes.make_cameras(4, seed * 1000 + i)).to(dev)
         imgs = torch.rand(4, 32, 32, 4, generator=g, device=dev)
-        dd, px = pg.generate_rays_batched(imgs, per_cam, T, 0.691, device=dev)
+        uv = torch.rand(4, per_cam, 2, generator=g, device=dev)
+        dd, px = pg.generate_rays_batched(imgs, per_cam, T, 0.691, device=dev, ray_uv=uv)
         oo = torch.repeat_interleave(T[:, :3, 3], per_cam, 0) + 2.0 * dd
         origins.append(oo[:n]); dirs.append(dd[:n]); targets.append(px[:n])
         owners.append(torch.full((n,), i, dtype=torch.int32, device=dev))
@@ -517,15 +539,14 @@ def precision_leg(pg, dev, steps, warmup):
         for i in range(warmup):
             st.step_cameras(T, imgs, P["camera_angle_x"], R, 5000 + i, near=P["near"])
         torch.cuda.synchronize(dev)
-        st.kernel_events = []
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0.record(stream)
-        for i in range(steps):
-            st.step_cameras(T, imgs, P["camera_angle_x"], R, 6000 + i, near=P["near"])
+        events = timed_launches(st, steps, lambda i: st.step_cameras(
+            T, imgs, P["camera_angle_x"], R, 6000 + i, near=P["near"]))
         t1.record(stream)
         torch.cuda.synchronize(dev)
         ms = t0.elapsed_time(t1) / steps
-        kern = sum(a.elapsed_time(b) for a, b in st.kernel_events) / steps
+        kern = mean_kernel_ms(events)
         out[name] = {"value": R / (ms / 1e3), "unit": "rays/s", "ms_per_step": ms, "kernel_ms": kern}
         del st, g
     out["bf16_over_f32_logsum"] = out["bf16_logsum"]["value"] / out["f32_logsum"]["value"]
@@ -610,18 +631,14 @@ def main():
         if world > 1:
             torch.distributed.barrier()
         launches0 = pg.launch_count()
-        step.kernel_events = []
         t0.record(stream)
-        for i in range(args.steps):
-            train(args.warmup + i)
+        kern_events = timed_launches(step, args.steps, lambda i: train(args.warmup + i))
         t1.record(stream)
         torch.cuda.synchronize(dev)
         launches = pg.launch_count() - launches0
-        kern_events = step.kernel_events
-        step.kernel_events = None
         load(0.3, 20_000)
     ms_total = t0.elapsed_time(t1)
-    kern_ms = sum(a.elapsed_time(b) for a, b in kern_events) / args.steps
+    kern_ms = mean_kernel_ms(kern_events)
     if world > 1:
         tt = torch.tensor([ms_total], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -635,9 +652,11 @@ def main():
     # are one copy; the step reads contiguous views of the device copy
     nb = 4
     host = []
+    uv_gen = torch.Generator(device=dev).manual_seed(7000 + rank)  # the same rays every run
     for b in range(nb):
+        uv = torch.rand(W["cameras"], R // W["cameras"] + 1, 2, device=dev, generator=uv_gen)
         dirs, pixels = pg.generate_rays_batched(imgs, R // W["cameras"] + 1, T, W["camera_angle_x"],
-                                                device=dev)
+                                                device=dev, ray_uv=uv)
         cam_pos = torch.repeat_interleave(T[:, :3, 3], R // W["cameras"] + 1, 0)
         o = cam_pos + W["near"] * dirs
         block = torch.cat([x[:R].reshape(-1) for x in (o, dirs, pixels)]).cpu().pin_memory()
@@ -726,7 +745,10 @@ def main():
                 "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES,
                 "traffic_unit": "bytes per launch (ncu capture of this workload)",
                 "kernel": "render_kernel<trilinear,train>",
-                "kernel_ms": kern_ms, "unique_cells": U, "algorithmic_bytes": alg_bytes,
+                "kernel_ms": kern_ms,
+                "kernel_ms_sample": f"CUDA events around every {KERNEL_EVENT_EVERY}th launch of the "
+                                    f"timed region ({len(kern_events)} launches)",
+                "unique_cells": U, "algorithmic_bytes": alg_bytes,
                 "unique_cells_definition": "distinct cells read by the step's in-bounds samples "
                                            "(all 8 corners), as the reference's algorithm reads them",
                 "unique_cells_live": U_live, "algorithmic_bytes_live": alg_live,
