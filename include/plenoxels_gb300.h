@@ -118,9 +118,11 @@ int pgb_render_bwd(const pgb_grid* grid, const pgb_rays* rays, const void* d_rgb
 /* Fused training step: forward, MSE against target (mean over R*4 entries times
  * loss_weight, scripts/train.py:156), and backward in one launch. target is [R,4] Real
  * (ignored when rays->cameras is set: targets are the sampled image pixels).
- * rgba_out may be NULL. loss_out[0] receives the loss (Real). workspace must hold
- * pgb_train_workspace_bytes() bytes and be zeroed once before first use; the kernel
- * leaves it zeroed again. */
+ * rgba_out may be NULL. loss_out[0] receives the loss (Real), written by the kernel:
+ * any address the GPU can store to, device memory or pinned host memory (under unified
+ * addressing a pinned host pointer is a device pointer), so a host reads the loss after
+ * the stream synchronises with no copy. workspace must hold pgb_train_workspace_bytes()
+ * bytes and be zeroed once before first use; the kernel leaves it zeroed again. */
 int pgb_render_train(const pgb_grid* grid, const pgb_rays* rays, const void* target,
                      double loss_weight, void* rgba_out, void* grad_cells, void* loss_out,
                      void* workspace, pgb_stream_t stream);
