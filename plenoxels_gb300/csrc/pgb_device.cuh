@@ -190,6 +190,11 @@ struct LossSum<float> {
   float hi = 0.f, lo = 0.f;
   __device__ __forceinline__ void add(float x) {
     const float s = hi + x;
+    if (isinf(s)) {  // an infinite sum carries no error term (inf - inf would make it NaN)
+      hi = s;
+      lo = 0.f;
+      return;
+    }
     const float b = s - hi;
     lo += (hi - (s - b)) + (x - b);
     hi = s;
